@@ -1,0 +1,86 @@
+// The engine object behind an iemic_ocean handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/iemic_gb300.h"
+#include "ocean_impl.cuh"
+
+namespace iemic {
+
+struct EngineError {
+    int code;
+    explicit EngineError(int c) : code(c) {}
+};
+inline void ck(cudaError_t e) {
+    if (e != cudaSuccess) throw EngineError(IEMIC_ERR_CUDA);
+}
+
+struct NdLu;   // nested-dissection block factorisation (ndlu.cu)
+
+struct Engine {
+    iemic_config cfg{};
+    size_t nc = 0;
+    int ndim = 0;
+    int64_t nnz = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+
+    // host-side geometry
+    double xmin = 0, xmax = 0, ymin = 0, ymax = 0, dx = 0, dy = 0, dz = 0, tdzi2 = 0;
+    std::vector<double> y, yv, z, dfzT, dfzW, jt, kt, surf;
+    std::vector<int> landm, row_ptr;
+    std::vector<int8_t> slot;
+
+    Params P{};
+    ForcingScalars fs{};
+    Geo geo{};
+    Pattern pat{};
+
+    // device buffers
+    int8_t* d_lm = nullptr;
+    int8_t* d_slot = nullptr;
+    double *d_jt = nullptr, *d_kt = nullptr, *d_al = nullptr, *d_pads = nullptr, *d_surf = nullptr;
+    double *d_x = nullptr, *d_F = nullptr, *d_v1 = nullptr, *d_v2 = nullptr, *d_B = nullptr;
+    int *d_rowptr = nullptr, *d_col = nullptr;
+    double* d_val = nullptr;
+    float* d_val32 = nullptr;
+
+    bool jac_valid = false;
+    bool fact_stale = true;
+
+    // solver state (krylov.cu / ndlu.cu)
+    NdLu* lu64 = nullptr;
+    NdLu* lu32 = nullptr;
+    struct Krylov* kry = nullptr;
+
+    ~Engine();
+    void init(const iemic_config& c, const int* landm_in);
+    void* dalloc(size_t bytes);
+    void build_grid();
+    void stpnt();
+    void update_forcing();
+    void lin();
+    void build_pattern();
+    void set_par(int idx, double value);
+    void rhs_dev(const double* x, double* F);
+    void jacobian_dev(const double* x);
+
+    // linear algebra (krylov.cu)
+    void spmv64(const double* x, double* y);
+    void spmv32(const float* x, float* y);
+    void free_solver();
+    void ensure_solver();
+    void build_preconditioner(int precision);
+    int solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);
+    void apply_precon(int precision, const double* v, double* out);
+};
+
+}  // namespace iemic
+
+// the opaque handle of include/iemic_gb300.h
+struct iemic_ocean {
+    iemic::Engine e;
+};

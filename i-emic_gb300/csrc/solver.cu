@@ -1,0 +1,87 @@
+// C ABI of the linear-solve path (Ocean::solve / applyPrecon /
+// buildPreconditioner, src/ocean/Ocean.C:1070-1147, 1377-1404).
+#include "engine.cuh"
+
+using namespace iemic;
+
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                            \
+    }                                                        \
+    catch (const EngineError& err) { return err.code; }      \
+    catch (...) { return IEMIC_ERR_CUDA; }                   \
+    return IEMIC_OK;
+
+extern "C" {
+
+void iemic_default_solve_opts(iemic_solve_opts* o) {
+    if (!o) return;
+    o->precision = IEMIC_PREC_MIXED;
+    o->restart = 100;          // Belos "Num Blocks" (FGMRES iterations)
+    o->max_iters = 1000;
+    o->tol = 1e-8;
+    o->max_refinements = 20;
+    o->inner_tol = 1e-4;
+    o->transpose = 0;
+}
+
+int iemic_build_preconditioner(iemic_ocean* h, int precision) {
+    if (!h || precision < -1 || precision > 1) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    if (!h->e.jac_valid) return IEMIC_ERR_STATE;
+    if (precision == -1 || precision == IEMIC_PREC_FP64) h->e.build_preconditioner(IEMIC_PREC_FP64);
+    if (precision == -1 || precision == IEMIC_PREC_MIXED) h->e.build_preconditioner(IEMIC_PREC_MIXED);
+    ck(cudaStreamSynchronize(h->e.stream));
+    GUARD_END
+}
+
+int iemic_apply_precon(iemic_ocean* h, int precision, const double* v, double* out) {
+    if (!h || !v || !out || precision < 0 || precision > 1) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    Engine& e = h->e;
+    ck(cudaMemcpyAsync(e.d_v1, v, sizeof(double) * e.ndim, cudaMemcpyHostToDevice, e.stream));
+    e.apply_precon(precision, e.d_v1, e.d_v2);
+    ck(cudaMemcpyAsync(out, e.d_v2, sizeof(double) * e.ndim, cudaMemcpyDeviceToHost, e.stream));
+    ck(cudaStreamSynchronize(e.stream));
+    GUARD_END
+}
+
+int iemic_solve_dev(iemic_ocean* h, const double* b, double* x, const iemic_solve_opts* o, iemic_solve_stats* st) {
+    if (!h || !b || !x) return IEMIC_ERR_ARG;
+    iemic_solve_opts oo;
+    iemic_default_solve_opts(&oo);
+    if (o) oo = *o;
+    if (oo.restart < 1 || oo.restart > 1000 || oo.max_iters < 1 || !(oo.tol > 0)) return IEMIC_ERR_ARG;
+    iemic_solve_stats s{};
+    int rc;
+    try {
+        rc = h->e.solve_dev(b, x, oo, s);
+        ck(cudaStreamSynchronize(h->e.stream));
+    } catch (const EngineError& err) {
+        rc = err.code;
+    } catch (...) {
+        rc = IEMIC_ERR_CUDA;
+    }
+    if (st) *st = s;
+    return rc;
+}
+
+int iemic_solve(iemic_ocean* h, const double* b, double* x, const iemic_solve_opts* o, iemic_solve_stats* st) {
+    if (!h || !b || !x) return IEMIC_ERR_ARG;
+    Engine& e = h->e;
+    try {
+        ck(cudaMemcpyAsync(e.d_v1, b, sizeof(double) * e.ndim, cudaMemcpyHostToDevice, e.stream));
+    } catch (...) {
+        return IEMIC_ERR_CUDA;
+    }
+    int rc = iemic_solve_dev(h, e.d_v1, e.d_v2, o, st);
+    try {
+        ck(cudaMemcpyAsync(x, e.d_v2, sizeof(double) * e.ndim, cudaMemcpyDeviceToHost, e.stream));
+        ck(cudaStreamSynchronize(e.stream));
+    } catch (...) {
+        return IEMIC_ERR_CUDA;
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,284 @@
+"""Host-side mirror of the reference's ``Ocean`` model API.
+
+Method names, argument meaning and the parameter names follow
+src/ocean/Ocean.H:169-250 and src/utils/Model.H:54-145:
+``computeRHS``, ``computeJacobian``, ``solve``, ``applyMatrix``,
+``applyPrecon``, ``applyMassMat``, ``getState/getRHS/getSolution(mode)``,
+``setPar/getPar(name)``. Errors from the C ABI raise ``IemicError`` (the
+reference throws ``std::runtime_error`` through its ``ERROR`` macro).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+# Parameter names of THCM::par2int (src/ocean/THCM.C:1841-1886)
+PARAMETER_NAMES = {
+    "AL_T": 1, "Rayleigh-Number": 2, "Vertical Ekman-Number": 3, "Horizontal Ekman-Number": 4,
+    "Rossby-Number": 5, "MIXP": 6, "RESC": 7, "SPL1": 8, "Salinity Homotopy": 9,
+    "Solar Forcing": 10, "Horizontal Peclet-Number": 11, "Vertical Peclet-Number": 12,
+    "P_VC": 13, "LAMB": 14, "Salinity Forcing": 15, "Wind Forcing": 16,
+    "Temperature Forcing": 17, "Nonlinear Factor": 18, "Combined Forcing": 19, "ARCL": 20,
+    "NLES": 21, "IFRICB": 22, "CONT": 23, "Energy": 24, "ALPC": 25, "CMPR": 26,
+    "Flux Perturbation": 27, "Salinity Perturbation": 28, "MKAP": 29, "SPL2": 30,
+}
+
+ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "not converged", -4: "NaN/Inf",
+          -5: "zero pivot", -6: "call order", -7: "device allocation failed"}
+
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class IemicError(RuntimeError):
+    def __init__(self, code, where):
+        self.code = code
+        super().__init__("%s failed: %s (%d)" % (where, ERRORS.get(code, "error"), code))
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("m", ctypes.c_int), ("l", ctypes.c_int),
+                ("xmin_deg", ctypes.c_double), ("xmax_deg", ctypes.c_double),
+                ("ymin_deg", ctypes.c_double), ("ymax_deg", ctypes.c_double),
+                ("periodic", ctypes.c_int), ("hdim", ctypes.c_double), ("qz", ctypes.c_double),
+                ("alphaT", ctypes.c_double), ("alphaS", ctypes.c_double),
+                ("ih", ctypes.c_int), ("coriolis_on", ctypes.c_int),
+                ("tres", ctypes.c_int), ("sres", ctypes.c_int),
+                ("iza", ctypes.c_int), ("ite", ctypes.c_int), ("its", ctypes.c_int),
+                ("forcing_type", ctypes.c_int)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("restart", ctypes.c_int), ("max_iters", ctypes.c_int),
+                ("tol", ctypes.c_double), ("max_refinements", ctypes.c_int),
+                ("inner_tol", ctypes.c_double), ("transpose", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int), ("refinements", ctypes.c_int), ("relres", ctypes.c_double),
+                ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
+
+
+# Every entry point of include/iemic_gb300.h with its ctypes signature.
+_VP = ctypes.c_void_p
+_IP = ctypes.POINTER(ctypes.c_int)
+_DP = ctypes.POINTER(ctypes.c_double)
+SIGNATURES = {
+    "iemic_create": [ctypes.POINTER(Config), _IP, ctypes.POINTER(_VP)],
+    "iemic_destroy": [_VP],
+    "iemic_ndim": [_VP, _IP],
+    "iemic_get_landm": [_VP, _IP],
+    "iemic_set_par": [_VP, ctypes.c_int, ctypes.c_double],
+    "iemic_get_par": [_VP, ctypes.c_int, _DP],
+    "iemic_set_forcing": [_VP, _DP, _DP, _DP, _DP, _DP],
+    "iemic_rhs": [_VP, _DP, _DP],
+    "iemic_jacobian": [_VP, _DP],
+    "iemic_rhs_dev": [_VP, _VP, _VP],
+    "iemic_jacobian_dev": [_VP, _VP],
+    "iemic_graph_nnz": [_VP, ctypes.POINTER(ctypes.c_int64)],
+    "iemic_get_csr": [_VP, _IP, _IP, _DP, ctypes.c_int],
+    "iemic_mass": [_VP, _DP],
+    "iemic_apply_matrix": [_VP, _DP, _DP],
+    "iemic_default_solve_opts": [ctypes.POINTER(SolveOpts)],
+    "iemic_build_preconditioner": [_VP, ctypes.c_int],
+    "iemic_apply_precon": [_VP, ctypes.c_int, _DP, _DP],
+    "iemic_solve": [_VP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats)],
+    "iemic_solve_dev": [_VP, _VP, _VP, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats)],
+}
+
+_lib = None
+
+
+def load_library(path=None, build_if_missing=True):
+    """Load libiemic_gb300.so (building it with nvcc if it is missing)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    if path is None:
+        path = _build.LIB
+        if build_if_missing and not os.path.exists(path):
+            _build.build()
+    L = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = None if name == "iemic_default_solve_opts" else ctypes.c_int
+    if path == _build.LIB:
+        _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+class Ocean:
+    """The THCM ocean model on one GPU (mirror of the reference ``Ocean``)."""
+
+    def __init__(self, config, landm=None, forcing=None, starting_parameters=()):
+        self.L = load_library()
+        self.config = dict(config)
+        c = Config(**{k: config[k] for k, _ in Config._fields_})
+        self._h = _VP()
+        lm = None
+        if landm is not None:
+            self._landm_in = np.ascontiguousarray(landm, dtype=np.int32).ravel()
+            lm = _ip(self._landm_in)
+        self._check(self.L.iemic_create(ctypes.byref(c), lm, ctypes.byref(self._h)), "iemic_create")
+        nd = ctypes.c_int()
+        self._check(self.L.iemic_ndim(self._h, ctypes.byref(nd)), "iemic_ndim")
+        self.ndim = nd.value
+        self.n, self.m, self.l = config["n"], config["m"], config["l"]
+        self.state = np.zeros(self.ndim)
+        self.rhs = np.zeros(self.ndim)
+        self.sol = np.zeros(self.ndim)
+        self._jac_state = None
+        if forcing:
+            self.setForcing(**forcing)
+        for name, val in starting_parameters:
+            self.setPar(name, val)
+
+    # ---- lifecycle ------------------------------------------------------
+    def _check(self, rc, where):
+        if rc != 0:
+            raise IemicError(rc, where)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.L.iemic_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- parameters and forcing ------------------------------------------
+    @staticmethod
+    def par2int(name):
+        if isinstance(name, int):
+            return name
+        if name not in PARAMETER_NAMES:
+            raise KeyError("unknown THCM parameter %r" % name)
+        return PARAMETER_NAMES[name]
+
+    def setPar(self, name, value):
+        self._check(self.L.iemic_set_par(self._h, self.par2int(name), float(value)), "setPar")
+
+    def getPar(self, name):
+        v = ctypes.c_double()
+        self._check(self.L.iemic_get_par(self._h, self.par2int(name), ctypes.byref(v)), "getPar")
+        return v.value
+
+    def setForcing(self, taux=None, tauy=None, tatm=None, emip=None, spert=None):
+        keep, ptrs = [], []
+        for a in (taux, tauy, tatm, emip, spert):
+            if a is None:
+                ptrs.append(None)
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+                if a.size != self.n * self.m:
+                    raise ValueError("forcing field must have n*m entries")
+                keep.append(a)
+                ptrs.append(_dp(a))
+        self._check(self.L.iemic_set_forcing(self._h, *ptrs), "setForcing")
+
+    def getLandMask(self):
+        out = np.zeros((self.l + 2) * (self.m + 2) * (self.n + 2), dtype=np.int32)
+        self._check(self.L.iemic_get_landm(self._h, _ip(out)), "getLandMask")
+        return out
+
+    # ---- Model API -------------------------------------------------------
+    def getState(self, mode="C"):
+        return self.state if mode == "V" else self.state.copy()
+
+    def getRHS(self, mode="C"):
+        return self.rhs if mode == "V" else self.rhs.copy()
+
+    def getSolution(self, mode="C"):
+        return self.sol if mode == "V" else self.sol.copy()
+
+    def setState(self, x):
+        self.state[:] = np.asarray(x, dtype=np.float64)
+
+    def computeRHS(self, x=None):
+        x = self.state if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(self.ndim)
+        self._check(self.L.iemic_rhs(self._h, _dp(x), _dp(out)), "computeRHS")
+        if x is self.state:
+            self.rhs[:] = out
+        return out
+
+    def computeJacobian(self, x=None):
+        x = self.state if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        self._check(self.L.iemic_jacobian(self._h, _dp(x)), "computeJacobian")
+
+    def graph_nnz(self):
+        v = ctypes.c_int64()
+        self._check(self.L.iemic_graph_nnz(self._h, ctypes.byref(v)), "graph_nnz")
+        return v.value
+
+    def getJacobian(self, index_base=0, values=True):
+        """(row_ptr, col_idx, values) of the maximal-graph CSR."""
+        nnz = self.graph_nnz()
+        rp = np.zeros(self.ndim + 1, dtype=np.int32)
+        ci = np.zeros(nnz, dtype=np.int32)
+        va = np.zeros(nnz) if values else None
+        self._check(self.L.iemic_get_csr(self._h, _ip(rp), _ip(ci), _dp(va) if values else None, index_base),
+                    "getJacobian")
+        return rp, ci, va
+
+    def getMassMat(self):
+        out = np.zeros(self.ndim)
+        self._check(self.L.iemic_mass(self._h, _dp(out)), "getMassMat")
+        return out
+
+    def applyMassMat(self, v):
+        return self.getMassMat() * np.asarray(v, dtype=np.float64)
+
+    def applyMatrix(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        out = np.zeros(self.ndim)
+        self._check(self.L.iemic_apply_matrix(self._h, _dp(v), _dp(out)), "applyMatrix")
+        return out
+
+    def default_solve_opts(self, precision=PREC_MIXED):
+        o = SolveOpts()
+        self.L.iemic_default_solve_opts(ctypes.byref(o))
+        o.precision = precision
+        return o
+
+    def buildPreconditioner(self, precision=-1):
+        self._check(self.L.iemic_build_preconditioner(self._h, precision), "buildPreconditioner")
+
+    def applyPrecon(self, v, precision=PREC_FP64):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        out = np.zeros(self.ndim)
+        self._check(self.L.iemic_apply_precon(self._h, precision, _dp(v), _dp(out)), "applyPrecon")
+        return out
+
+    def solve(self, rhs=None, opts=None, **kw):
+        """Ocean::solve: x = J^{-1} rhs (default rhs: the stored RHS)."""
+        b = self.rhs if rhs is None else np.ascontiguousarray(rhs, dtype=np.float64)
+        o = opts if opts is not None else self.default_solve_opts(kw.pop("precision", PREC_MIXED))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        x = np.zeros(self.ndim)
+        st = SolveStats()
+        rc = self.L.iemic_solve(self._h, _dp(b), _dp(x), ctypes.byref(o), ctypes.byref(st))
+        stats = dict(iters=st.iters, refinements=st.refinements, relres=st.relres,
+                     time_factor_ms=st.time_factor_ms, time_solve_ms=st.time_solve_ms, status=rc)
+        if rc not in (0, -3):
+            raise IemicError(rc, "solve")
+        self.sol[:] = x
+        return x, stats

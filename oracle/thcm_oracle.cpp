@@ -1,0 +1,1330 @@
+// CPU oracle for the THCM Newton-step path (TEST INFRASTRUCTURE ONLY).
+//
+// FP64 restatement of the reference's Fortran physics. Each routine cites the
+// reference routine it follows. Whole-array Fortran expressions are evaluated
+// element by element in the same left-to-right order, and this file must be
+// compiled with -ffp-contract=off so no fused multiply-adds change rounding
+// (the reference's gfortran -O3 build on x86-64 emits none either).
+// Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU baseline.
+#include "thcm_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// ---- constants: src/ocean/par.F90:11-83, usr.F90:130-171, atm.F90 ----------
+constexpr double PI = 3.14159265358979323846;
+constexpr int NUN = 6, NP = 27, NPAR = 30;
+enum { UU = 1, VV = 2, WW = 3, PP = 4, TT = 5, SS = 6 };
+enum { OCEAN = 0, LAND = 1, WATER = 2, PERIO = 3 };
+enum {
+    AL_T = 1, RAYL, EK_V, EK_H, ROSB, MIXP, RESC, SPL1, HMTP, SUNP, PE_H, PE_V, P_VC,
+    LAMB, SALT, WIND, TEMP, BIOT, COMB, ARCL, NLES, IFRICB, CONT, ENER, ALPC, CMPR,
+    FPER, SPER, MKAP, SPL2
+};
+constexpr double omegadim = 7.292e-05, r0dim = 6.37e+06, udim = 0.1e+00,
+                 gdim = 9.8e+00, rhodim = 1.024e+03, deltas = 1.0, s0 = 35.0,
+                 cp0 = 4.2e+03, alpt1 = 2.93, alpt2 = 8.3e-02, alpt3 = 6.6e-04,
+                 ah = 2.5e+05, av = 1.0e-03, kappah = 1.0e+03, kappav = 1.0e-04;
+constexpr double zmin = -1.0, zmax = 0.0;
+
+// Fortran-style array with arbitrary lower bounds, column-major.
+struct Arr3 {
+    int i0, i1, j0, j1, k0, k1, ni, nj;
+    std::vector<double> d;
+    Arr3() = default;
+    Arr3(int a0, int a1, int b0, int b1, int c0, int c1)
+        : i0(a0), i1(a1), j0(b0), j1(b1), k0(c0), k1(c1), ni(a1 - a0 + 1), nj(b1 - b0 + 1),
+          d(size_t(ni) * nj * (c1 - c0 + 1), 0.0) {}
+    double& operator()(int i, int j, int k) {
+        return d[size_t(i - i0) + size_t(ni) * (size_t(j - j0) + size_t(nj) * size_t(k - k0))];
+    }
+    void zero() { std::fill(d.begin(), d.end(), 0.0); }
+};
+
+struct Model {
+    // configuration
+    int n, m, l, ndim;
+    bool periodic;
+    double xmin, xmax, ymin, ymax, hdim, qz, alphaT, alphaS;
+    int ih, coriolis_on, TRES, SRES, iza, ite, its, forcing_type;
+    const int coupled_T = 0, coupled_S = 0;
+    // grid (src/ocean/grid.F90)
+    double dx, dy, dz;
+    std::vector<double> x, y, xu, yv, z, zw, ze, zwe, dfzT, dfzW;  // offset storage below
+    std::vector<int> landm;
+    double par[NPAR + 1];
+    double QTnd, QSnd;
+    std::vector<double> Frc, taux, tauy, tatm, emip, spert, adapted_emip, internal_temp,
+        internal_salt;
+    std::vector<double> Al, An;
+    std::vector<int> begA, jcoA;
+    std::vector<double> coA, coB;
+    // maximal graph
+    std::vector<int> g_ptr, g_col;
+
+    // ---- index helpers ----
+    double& Y(int j) { return y[j]; }            // y(0:m+1)
+    double& YV(int j) { return yv[j]; }          // yv(0:m)
+    double& XU(int i) { return xu[i]; }          // xu(0:n)
+    double& DFZT(int k) { return dfzT[k - 1]; }  // dfzT(1:l)
+    double& DFZW(int k) { return dfzW[k]; }      // dfzW(0:l)
+    double& ZW(int k) { return zw[k]; }          // zw(0:l)
+    double& Z(int k) { return z[k - 1]; }
+    int& LM(int i, int j, int k) { return landm[i + (n + 2) * (j + (m + 2) * k)]; }
+    int find_row2(int i, int j, int k, int XX) const {
+        return NUN * ((k - 1) * n * m + n * (j - 1) + i - 1) + XX;
+    }
+    size_t cell(int i, int j, int k) const {
+        return size_t(i - 1) + size_t(n) * (size_t(j - 1) + size_t(m) * size_t(k - 1));
+    }
+    size_t aidx(int kk, int A, int B, int i, int j, int k) const {
+        return size_t(kk - 1) + NP * (size_t(A - 1) + NUN * (size_t(B - 1) + NUN * cell(i, j, k)));
+    }
+    double& AN(int kk, int A, int B, int i, int j, int k) { return An[aidx(kk, A, B, i, j, k)]; }
+    double& AL(int kk, int A, int B, int i, int j, int k) { return Al[aidx(kk, A, B, i, j, k)]; }
+    double& F2(std::vector<double>& f, int i, int j) { return f[size_t(i - 1) + size_t(n) * (j - 1)]; }
+    double& F3(std::vector<double>& f, int i, int j, int k) {
+        return f[size_t(i - 1) + size_t(n) * (size_t(j - 1) + size_t(m) * (k - 1))];
+    }
+
+    // atom(np,n,m,l)
+    struct Atom {
+        int n, m, l;
+        std::vector<double> d;
+        Atom(int n_, int m_, int l_) : n(n_), m(m_), l(l_), d(size_t(NP) * n_ * m_ * l_, 0.0) {}
+        double& operator()(int kk, int i, int j, int k) {
+            return d[size_t(kk - 1) + NP * (size_t(i - 1) + size_t(n) * (size_t(j - 1) + size_t(m) * (k - 1)))];
+        }
+        void zero() { std::fill(d.begin(), d.end(), 0.0); }
+    };
+    Atom mk() { return Atom(n, m, l); }
+
+    // ---- src/ocean/spf.F90:792-854 ----
+    double amh(double yy) const { return ih == 0 ? 1.0 : 1. + 10.0 * std::exp(-5 * yy * yy); }
+    double bmh(double yy) const { return ih == 0 ? 1.0 : 1.0 + 10.0 * std::exp(-5 * yy * yy); }
+    double bmhy(double yy) const { return ih == 0 ? 0.0 : -10. * 10.0 * yy * std::exp(-5 * yy * yy); }
+
+    // ---- grid: src/ocean/grid.F90:2-95 ----
+    static double fz(double zz, double q) {
+        double th = std::tanh(q * (zz + 1));
+        double tth = std::tanh(q);
+        if (q > 1.0) return -1 + th / tth;
+        return zz + (1. - q) * zz * (1 - zz);
+    }
+    static double dfdz(double zz, double q) {
+        double ch = std::cosh(q * (zz + 1));
+        double tth = std::tanh(q);
+        if (q > 1.0) return q / (tth * ch * ch);
+        return 1.0 + (1. - q) * (1. - 2. * zz);
+    }
+    void grid() {
+        dx = (xmax - xmin) / n;
+        dy = (ymax - ymin) / m;
+        dz = (zmax - zmin) / l;
+        x.assign(n, 0);
+        xu.assign(n + 1, 0);
+        y.assign(m + 2, 0);
+        yv.assign(m + 1, 0);
+        z.assign(l, 0);
+        zw.assign(l + 1, 0);
+        ze.assign(l, 0);
+        zwe.assign(l, 0);
+        dfzT.assign(l, 0);
+        dfzW.assign(l + 1, 0);
+        for (int i = 1; i <= n; ++i) {
+            x[i - 1] = (double(i) - 0.5) * dx + xmin;
+            xu[i] = (double(i)) * dx + xmin;
+        }
+        xu[0] = xmin;
+        for (int j = 1; j <= m; ++j) {
+            y[j] = (double(j) - 0.5) * dy + ymin;
+            yv[j] = (double(j)) * dy + ymin;
+        }
+        y[0] = y[1] - dy;
+        y[m + 1] = y[m] + dy;
+        yv[0] = ymin;
+        for (int k = 1; k <= l; ++k) {
+            ze[k - 1] = (double(k) - 0.5) * dz + zmin;
+            zwe[k - 1] = (double(k)) * dz + zmin;
+            z[k - 1] = fz(ze[k - 1], qz);
+            zw[k] = fz(zwe[k - 1], qz);
+            dfzT[k - 1] = dfdz(ze[k - 1], qz);
+            dfzW[k] = dfdz(zwe[k - 1], qz);
+        }
+        zw[0] = zmin;
+        dfzW[0] = dfdz(zmin, qz);
+    }
+
+    // ---- stpnt: src/ocean/usrc.F90:1153-1197 (+ vmix_par with vmix=0) ----
+    void stpnt() {
+        for (int i = 0; i <= NPAR; ++i) par[i] = 0.0;
+        par[AL_T] = 0.1 / (2 * omegadim * rhodim * hdim * udim * dz * DFZT(l));
+        par[RAYL] = alphaT * gdim * hdim / (2 * omegadim * udim * r0dim);
+        par[EK_V] = av / (2 * omegadim * hdim * hdim);
+        par[EK_H] = ah / (2 * omegadim * r0dim * r0dim);
+        par[ROSB] = udim / (2 * omegadim * r0dim);
+        par[HMTP] = 0.0;
+        par[SUNP] = 0.0;
+        par[PE_H] = kappah / (udim * r0dim);
+        par[PE_V] = kappav * r0dim / (udim * hdim * hdim);
+        par[P_VC] = 2.5e+04 * par[PE_V];
+        par[LAMB] = alphaS / alphaT;
+        par[SALT] = 0.0;
+        par[WIND] = 0.0;
+        par[TEMP] = 0.0;
+        par[BIOT] = r0dim / (75. * 3600. * 24. * udim);
+        par[COMB] = 0.0;
+        par[NLES] = 0.0;
+        par[CMPR] = 0.0;
+        par[ALPC] = 1.0;
+        par[ENER] = 1.0e+02;
+        par[MIXP] = 0.0;
+        par[MKAP] = 0.0;
+        par[SPL1] = 2.0e+03;
+        par[SPL2] = 0.01;
+        // vmix_par (src/ocean/mix_imp.f:113-128) with Mixing = 0
+        par[MIXP] = 0.0;
+        par[P_VC] = 0.0;
+        par[ALPC] = 1.0;
+        par[ENER] = 1.0e+2;
+        par[MKAP] = 0.0;
+    }
+
+    // ---- forcing profiles: src/ocean/forcing.F90:405-449 ----
+    double wfun(double yy, int v1) const {
+        if (v1 == 1)
+            return 0.2 - 0.8 * std::sin(6 * std::fabs(yy)) - 0.5 * (1 - std::tanh(10 * std::fabs(yy))) -
+                   0.5 * (1 - std::tanh(10 * (PI / 2 - std::fabs(yy))));
+        return 0.0;
+    }
+    double temfun(double yy) {
+        if (forcing_type == 2) return std::cos(PI * (yy - ymin) / (ymax - ymin));
+        return std::cos(PI * yy / ymax) + par[CMPR] * std::sin(PI * yy / ymax);
+    }
+    double salfun(double yy) {
+        if (forcing_type == 2) return std::cos(PI * (yy - ymin) / (ymax - ymin));
+        if (forcing_type == 1) return (std::cos(PI * yy / ymax) + par[FPER] * yy / ymax) / std::cos(yy);
+        return std::cos(PI * yy / ymax) + par[FPER] * yy / ymax;
+    }
+
+    // ---- forcing: src/ocean/forcing.F90:4-218 (uncoupled, restoring branches) ----
+    void forcing() {
+        std::fill(Frc.begin(), Frc.end(), 0.0);
+        double sigma = par[COMB] * par[WIND] * par[AL_T];
+        if (iza == 2) {
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= n; ++i) {
+                    F2(taux, i, j) = wfun(YV(j), 1);
+                    F2(tauy, i, j) = wfun(YV(j), 2);
+                }
+        }
+        for (int j = 1; j <= m - 1; ++j)
+            for (int i = 1; i <= n; ++i) {
+                Frc[find_row2(i, j, l, UU) - 1] = sigma * F2(taux, i, j);
+                Frc[find_row2(i, j, l, VV) - 1] = sigma * F2(tauy, i, j);
+            }
+        double etabi = par[COMB] * par[TEMP] * (double(1 - TRES) + TRES * par[BIOT]);
+        double temcor = 0.0;
+        if (ite == 1 && coupled_T == 0) {
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= n; ++i) F2(tatm, i, j) = temfun(Y(j));
+            // TRES == 0 would call qint: restoring-only path here.
+        }
+        for (int j = 1; j <= m; ++j)
+            for (int i = 1; i <= n; ++i)
+                Frc[find_row2(i, j, l, TT) - 1] = etabi * (F2(tatm, i, j) - temcor);
+
+        double gamma = par[COMB] * par[SALT] * (double(1 - SRES) + SRES * par[BIOT]);
+        double salcor = 0.0;
+        if (its == 1) {
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= n; ++i) F2(emip, i, j) = salfun(Y(j)) * double(1 - LM(i, j, l));
+        }
+        double adapted_salcor = 0.0, spertcor = 0.0;
+        for (int j = 1; j <= m; ++j)
+            for (int i = 1; i <= n; ++i)
+                Frc[find_row2(i, j, l, SS) - 1] =
+                    gamma * (1 - par[HMTP]) * (F2(emip, i, j) - salcor) +
+                    gamma * par[HMTP] * (F2(adapted_emip, i, j) - adapted_salcor) +
+                    par[SPER] * (double(1 - SRES) + SRES * par[BIOT]) * (F2(spert, i, j) - spertcor);
+        for (int k = 1; k <= l - 1; ++k)
+            for (int j = 1; j <= m; ++j)
+                for (int i = 1; i <= n; ++i)
+                    Frc[find_row2(i, j, k, WW) - 1] =
+                        -(par[COMB] * double(1 - LM(i, j, k)) * par[RAYL] *
+                          (par[LAMB] * (F3(internal_salt, i, j, k) + F3(internal_salt, i, j, k + 1)) / 2. -
+                           (F3(internal_temp, i, j, k) + F3(internal_temp, i, j, k + 1)) / 2.));
+    }
+
+    // ---- spf.F90 derivative atoms ----
+    void uderiv(int type, Atom& a) {
+        a.zero();
+        switch (type) {
+        case 1:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) a(5, i, j, k) = 1.0;
+            break;
+        case 2: {
+            std::vector<double> c(m + 1);
+            for (int j = 0; j <= m; ++j) { double t = 1.0 / (std::cos(YV(j)) * dx); c[j] = t * t; }
+            for (int j = 1; j <= m - 1; ++j) for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) {
+                a(2, i, j, k) = amh(YV(j)) * c[j];
+                a(8, i, j, k) = amh(YV(j)) * c[j];
+                a(5, i, j, k) = -(a(2, i, j, k) + a(8, i, j, k));
+            }
+        } break;
+        case 3: {
+            double t = 1.0 / dy, r = t * t;
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m - 1; ++j) for (int k = 1; k <= l; ++k) {
+                a(4, i, j, k) = r * bmh(Y(j)) * std::cos(Y(j)) / std::cos(YV(j));
+                a(6, i, j, k) = r * bmh(Y(j + 1)) * std::cos(Y(j + 1)) / std::cos(YV(j));
+                a(5, i, j, k) = -(a(4, i, j, k) + a(6, i, j, k));
+            }
+        } break;
+        case 4: {
+            double t = 1.0 / dz, r = t * t;
+            for (int k = 1; k <= l; ++k) {
+                double h1 = 1. / (DFZT(k) * DFZW(k));
+                double h2 = 1. / (DFZT(k) * DFZW(k - 1));
+                for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                    a(14, i, j, k) = h2 * r;
+                    a(23, i, j, k) = h1 * r;
+                    a(5, i, j, k) = -(a(14, i, j, k) + a(23, i, j, k));
+                }
+            }
+        } break;
+        case 5:
+            for (int j = 1; j <= m - 1; ++j) {
+                double tv = std::tan(YV(j));
+                double tand2 = 1 - tv * tv;
+                double val = bmh(YV(j)) * tand2 + std::tan(YV(j)) * bmhy(YV(j));
+                for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) a(5, i, j, k) = val;
+            }
+            break;
+        case 6:
+            for (int j = 1; j <= m - 1; ++j) {
+                double tand2 = std::tan(YV(j)), cosd2 = std::cos(YV(j));
+                double num = bmhy(YV(j)) - (amh(YV(j)) + bmh(YV(j))) * tand2;
+                double v2 = num / (dx * cosd2);
+                double v8 = -(num / (dx * cosd2));
+                for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) { a(2, i, j, k) = v2; a(8, i, j, k) = v8; }
+            }
+            break;
+        }
+    }
+    void vderiv(int type, Atom& a) {
+        a.zero();
+        switch (type) {
+        case 1:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) a(5, i, j, k) = 1.0;
+            break;
+        case 2: {
+            std::vector<double> c(m + 1);
+            for (int j = 0; j <= m; ++j) { double t = 1.0 / (std::cos(YV(j)) * dx); c[j] = t * t; }
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m - 1; ++j) for (int k = 1; k <= l; ++k) {
+                a(2, i, j, k) = bmh(YV(j)) * c[j];
+                a(5, i, j, k) = -(2 * bmh(YV(j)) * c[j]);
+                a(8, i, j, k) = bmh(YV(j)) * c[j];
+            }
+        } break;
+        case 3: {
+            double t = 1.0 / dy, r = t * t;
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m - 1; ++j) for (int k = 1; k <= l; ++k) {
+                a(4, i, j, k) = r * amh(Y(j)) * std::cos(Y(j)) / std::cos(YV(j));
+                a(6, i, j, k) = r * amh(Y(j + 1)) * std::cos(Y(j + 1)) / std::cos(YV(j));
+                a(5, i, j, k) = -(a(4, i, j, k) + a(6, i, j, k));
+            }
+        } break;
+        case 4:
+            uderiv(4, a);
+            break;
+        case 5:
+            for (int j = 1; j <= m - 1; ++j) {
+                double tv = std::tan(YV(j));
+                double val = bmh(YV(j)) - amh(YV(j)) * tv * tv + bmhy(YV(j)) * tv;
+                for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) a(5, i, j, k) = val;
+            }
+            break;
+        case 6:
+            for (int j = 1; j <= m - 1; ++j) {
+                double tand2 = std::tan(YV(j)), cosd2 = std::cos(YV(j));
+                double num = (amh(YV(j)) + bmh(YV(j))) * tand2 - bmhy(YV(j));
+                double v2 = -(num / (dx * cosd2));
+                double v8 = num / (dx * cosd2);
+                for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) { a(2, i, j, k) = v2; a(8, i, j, k) = v8; }
+            }
+            break;
+        }
+    }
+    void pderiv(int type, Atom& a) {
+        a.zero();
+        switch (type) {
+        case 1:
+            for (int j = 1; j <= m; ++j) {
+                double c = 1.0 / (2 * std::cos(Y(j)) * dx);
+                for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) {
+                    a(2, i, j, k) = -c; a(4, i, j, k) = c; a(1, i, j, k) = -c; a(5, i, j, k) = c;
+                }
+            }
+            break;
+        case 2:
+            for (int j = 1; j <= m; ++j) {
+                double c = 1. / (2 * std::cos(Y(j)) * dy);
+                double cm = std::cos(YV(j - 1)), cc = std::cos(YV(j));
+                for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) {
+                    a(4, i, j, k) = -(cm * c);
+                    a(2, i, j, k) = cc * c;
+                    a(1, i, j, k) = -(cm * c);
+                    a(5, i, j, k) = cc * c;
+                }
+            }
+            break;
+        case 3: {
+            double dzi = 1.0 / dz;
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                a(5, i, j, k) = dzi / DFZT(k);
+                a(14, i, j, k) = -(dzi / DFZT(k));
+            }
+        } break;
+        }
+    }
+    void tderiv(int type, Atom& a) {
+        a.zero();
+        switch (type) {
+        case 1:
+        case 2:
+            for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) a(5, i, j, l) = 1.0;
+            break;
+        case 3:
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) {
+                double t = 1.0 / (std::cos(Y(j)) * dx), c = t * t;
+                double lm = double(1 - LM(i, j, l));
+                for (int k = 1; k <= l; ++k) {
+                    a(2, i, j, k) = c * lm;
+                    a(5, i, j, k) = -(2 * c * lm);
+                    a(8, i, j, k) = c * lm;
+                }
+            }
+            break;
+        case 4: {
+            double t = 1.0 / dy, d = t * t;
+            for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) {
+                double lm = double(1 - LM(i, j, l));
+                a(4, i, j, k) = (d * std::cos(YV(j - 1)) / std::cos(Y(j))) * lm;
+                a(6, i, j, k) = (d * std::cos(YV(j)) / std::cos(Y(j))) * lm;
+                a(5, i, j, k) = -(a(4, i, j, k) + a(6, i, j, k));
+            }
+        } break;
+        case 5: {
+            double t = 1.0 / dz, d = t * t;
+            for (int k = 1; k <= l - 1; ++k) {
+                double h1 = 1. / (DFZT(k) * DFZW(k));
+                double h2 = 1. / (DFZT(k) * DFZW(k - 1));
+                for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                    double lm = double(1 - LM(i, j, l));
+                    a(14, i, j, k) = h2 * d * lm;
+                    a(23, i, j, k) = h1 * d * lm;
+                    a(5, i, j, k) = -(a(14, i, j, k) + a(23, i, j, k));
+                }
+            }
+            int k = l;
+            double h2 = 1. / (DFZT(k) * DFZW(k - 1));
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) {
+                double lm = double(1 - LM(i, j, l));
+                a(14, i, j, k) = h2 * d * lm;
+                a(23, i, j, k) = 0.0;
+                a(5, i, j, k) = -(a(14, i, j, k) + a(23, i, j, k));
+            }
+        } break;
+        case 6:
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) for (int k = 1; k <= l; ++k) {
+                double lm = double(1 - LM(i, j, l));
+                a(23, i, j, k) = 1.0 * lm;
+                a(5, i, j, k) = 1.0 * lm;
+            }
+            break;
+        case 7:
+            for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) a(5, i, j, 1) = 1.0;
+            break;
+        }
+    }
+    void coriolis(int /*type*/, Atom& a) {
+        a.zero();
+        for (int j = 1; j <= m - 1; ++j) {
+            double corv = std::sin(YV(j)) * coriolis_on;
+            for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) a(5, i, j, k) = corv;
+        }
+    }
+    void gradp(int type, Atom& a) {
+        a.zero();
+        switch (type) {
+        case 1:
+            for (int j = 1; j <= m - 1; ++j) {
+                double c = 1. / (2 * std::cos(YV(j)) * dx);
+                for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) {
+                    a(5, i, j, k) = -c; a(6, i, j, k) = -c; a(8, i, j, k) = c; a(9, i, j, k) = c;
+                }
+            }
+            break;
+        case 2: {
+            double dyi = 1. / (2 * dy);
+            for (int i = 1; i <= n; ++i) for (int j = 1; j <= m - 1; ++j) for (int k = 1; k <= l; ++k) {
+                a(5, i, j, k) = -dyi; a(8, i, j, k) = -dyi; a(6, i, j, k) = dyi; a(9, i, j, k) = dyi;
+            }
+        } break;
+        case 3: {
+            double dzi = 1. / dz;
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                a(5, i, j, k) = -(dzi / DFZW(k));
+                a(23, i, j, k) = dzi / DFZW(k);
+            }
+        } break;
+        }
+    }
+
+    // Writes Al(:,A,B,:,:,1:l) = value(kk,i,j,k) for all entries.
+    template <class F>
+    void setAl(int A, int B, F f) {
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+            for (int kk = 1; kk <= NP; ++kk) AL(kk, A, B, i, j, k) = f(kk, i, j, k);
+    }
+    template <class F>
+    void addAn(int A, int B, F f) {
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+            for (int kk = 1; kk <= NP; ++kk) {
+                double& r = AN(kk, A, B, i, j, k);
+                r = f(r, kk, i, j, k);
+            }
+    }
+
+    // ---- lin: src/ocean/usrc.F90:605-789 (uncoupled branch) ----
+    void lin() {
+        Atom ucsi = mk(), uxx = mk(), uyy = mk(), uzz = mk(), uxs = mk(), fu = mk(), px = mk(), sc = mk(),
+             tcb = mk();
+        double EV = par[EK_V], EH = par[EK_H], ph = (1 - par[MIXP]) * par[PE_H], pv = par[PE_V],
+               lambda = par[LAMB], xes = par[NLES], bi = par[BIOT], Ra = par[RAYL];
+        std::fill(Al.begin(), Al.end(), 0.0);
+        // u-equation
+        uderiv(2, uxx); uderiv(3, uyy); uderiv(4, uzz); uderiv(5, ucsi); uderiv(6, uxs);
+        coriolis(1, fu); gradp(1, px);
+        setAl(UU, UU, [&](int kk, int i, int j, int k) {
+            return -EH * (uxx(kk, i, j, k) + uyy(kk, i, j, k) + ucsi(kk, i, j, k)) - EV * uzz(kk, i, j, k);
+        });
+        setAl(UU, VV, [&](int kk, int i, int j, int k) { return -fu(kk, i, j, k) - EH * uxs(kk, i, j, k); });
+        setAl(UU, PP, [&](int kk, int i, int j, int k) { return px(kk, i, j, k); });
+        // v-equation
+        vderiv(2, uxx); vderiv(3, uyy); vderiv(4, uzz); vderiv(5, ucsi); vderiv(6, uxs);
+        coriolis(2, fu); gradp(2, px);
+        setAl(VV, UU, [&](int kk, int i, int j, int k) { return fu(kk, i, j, k) - EH * uxs(kk, i, j, k); });
+        setAl(VV, VV, [&](int kk, int i, int j, int k) {
+            return -EH * (uxx(kk, i, j, k) + uyy(kk, i, j, k) + ucsi(kk, i, j, k)) - EV * uzz(kk, i, j, k);
+        });
+        setAl(VV, PP, [&](int kk, int i, int j, int k) { return px(kk, i, j, k); });
+        // w-equation
+        gradp(3, px); tderiv(6, uxs);
+        setAl(WW, PP, [&](int kk, int i, int j, int k) { return px(kk, i, j, k); });
+        setAl(WW, TT, [&](int kk, int i, int j, int k) { return -Ra * (1. + xes * alpt1) * uxs(kk, i, j, k) / 2.; });
+        setAl(WW, SS, [&](int kk, int i, int j, int k) { return lambda * Ra * uxs(kk, i, j, k) / 2.; });
+        // p-equation
+        pderiv(1, uxx); pderiv(2, uyy); pderiv(3, uzz);
+        setAl(PP, UU, [&](int kk, int i, int j, int k) { return uxx(kk, i, j, k); });
+        setAl(PP, VV, [&](int kk, int i, int j, int k) { return uyy(kk, i, j, k); });
+        setAl(PP, WW, [&](int kk, int i, int j, int k) { return uzz(kk, i, j, k); });
+        // T-equation
+        tderiv(1, fu); tderiv(2, sc); tderiv(3, uxx); tderiv(4, uyy); tderiv(5, uzz); tderiv(7, tcb);
+        setAl(TT, TT, [&](int kk, int i, int j, int k) {
+            return -ph * (uxx(kk, i, j, k) + uyy(kk, i, j, k)) - pv * uzz(kk, i, j, k) + TRES * bi * fu(kk, i, j, k);
+        });
+        // S-equation
+        setAl(SS, SS, [&](int kk, int i, int j, int k) {
+            return -ph * (uxx(kk, i, j, k) + uyy(kk, i, j, k)) - pv * uzz(kk, i, j, k) + SRES * bi * sc(kk, i, j, k);
+        });
+    }
+
+    // ---- usol: src/ocean/usrc.F90:1014-1121 ----
+    Arr3 u, v, w, p, t, s;
+    void usol(const double* un) {
+        u = Arr3(0, n, 0, m, 0, l + 1); v = Arr3(0, n, 0, m, 0, l + 1);
+        w = Arr3(0, n + 1, 0, m + 1, 0, l); p = Arr3(0, n + 1, 0, m + 1, 0, l + 1);
+        t = Arr3(0, n + 1, 0, m + 1, 0, l + 1); s = Arr3(0, n + 1, 0, m + 1, 0, l + 1);
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            u(i, j, k) = un[find_row2(i, j, k, UU) - 1];
+            v(i, j, k) = un[find_row2(i, j, k, VV) - 1];
+            w(i, j, k) = un[find_row2(i, j, k, WW) - 1];
+            p(i, j, k) = un[find_row2(i, j, k, PP) - 1];
+            t(i, j, k) = un[find_row2(i, j, k, TT) - 1];
+            s(i, j, k) = un[find_row2(i, j, k, SS) - 1];
+        }
+        const int N = n, M = m;
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) {
+            if (periodic) {
+                u(0, j, k) = u(N, j, k); v(0, j, k) = v(N, j, k);
+                w(N + 1, j, k) = w(1, j, k); w(0, j, k) = w(N, j, k);
+                p(N + 1, j, k) = p(1, j, k); p(0, j, k) = p(N, j, k);
+                t(N + 1, j, k) = t(1, j, k); t(0, j, k) = t(N, j, k);
+                s(N + 1, j, k) = s(1, j, k); s(0, j, k) = s(N, j, k);
+            } else {
+                u(0, j, k) = 0.0; u(N, j, k) = 0.0; v(0, j, k) = 0.0; v(N, j, k) = 0.0;
+                p(0, j, k) = 0.0; p(N + 1, j, k) = 0.0;
+                t(0, j, k) = t(1, j, k); t(N + 1, j, k) = t(N, j, k);
+                s(0, j, k) = s(1, j, k); s(N + 1, j, k) = s(N, j, k);
+            }
+        }
+        for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) {
+            u(i, 0, k) = 0.0; u(i, M, k) = 0.0; v(i, 0, k) = 0.0; v(i, M, k) = 0.0;
+            p(i, 0, k) = 0.0; p(i, M + 1, k) = 0.0;
+            t(i, 0, k) = t(i, 1, k); t(i, M + 1, k) = t(i, M, k);
+            s(i, 0, k) = s(i, 1, k); s(i, M + 1, k) = s(i, M, k);
+        }
+        for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            u(i, j, 0) = u(i, j, 1); u(i, j, l + 1) = u(i, j, l);
+            v(i, j, 0) = v(i, j, 1); v(i, j, l + 1) = v(i, j, l);
+            w(i, j, l) = 0.0; w(i, j, 0) = 0.0;
+            p(i, j, l + 1) = 0.0; p(i, j, 0) = 0.0;
+            t(i, j, l + 1) = t(i, j, l); t(i, j, 0) = t(i, j, 1);
+            s(i, j, l + 1) = s(i, j, l); s(i, j, 0) = s(i, j, 1);
+        }
+        for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) for (int k = 1; k <= l; ++k)
+            if (LM(i, j, k) == 1) {
+                u(i, j, k) = 0.0; v(i, j, k) = 0.0; u(i - 1, j, k) = 0.0; v(i - 1, j, k) = 0.0;
+                u(i, j - 1, k) = 0.0; v(i, j - 1, k) = 0.0; u(i - 1, j - 1, k) = 0.0; v(i - 1, j - 1, k) = 0.0;
+            }
+    }
+
+    // ---- tnlin: src/ocean/spf.F90:362-484 ----
+    void tnlin(int type, Atom& a, Arr3& U, Arr3& V, Arr3& W, Arr3& T) {
+        a.zero();
+        switch (type) {
+        case 2:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double c = 1.0 / (4 * std::cos(Y(j)) * dx), lm = double(1 - LM(i, j, l));
+                a(2, i, j, k) = -(T(i, j, k) + T(i - 1, j, k)) * c * lm;
+                a(4, i, j, k) = (T(i + 1, j, k) + T(i, j, k)) * c * lm;
+                a(1, i, j, k) = -(T(i, j, k) + T(i - 1, j, k)) * c * lm;
+                a(5, i, j, k) = (T(i + 1, j, k) + T(i, j, k)) * c * lm;
+            }
+            break;
+        case 3:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double c = 1.0 / (4 * std::cos(Y(j)) * dx), lm = double(1 - LM(i, j, l));
+                a(2, i, j, k) = -(U(i - 1, j, k) + U(i - 1, j - 1, k)) * c * lm;
+                a(8, i, j, k) = (U(i, j, k) + U(i, j - 1, k)) * c * lm;
+                a(5, i, j, k) = a(2, i, j, k) + a(8, i, j, k);
+            }
+            break;
+        case 4:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double c = 1.0 / (4 * std::cos(Y(j)) * dy), lm = double(1 - LM(i, j, l));
+                a(4, i, j, k) = -c * (T(i, j, k) + T(i, j - 1, k)) * std::cos(YV(j - 1)) * lm;
+                a(1, i, j, k) = -c * (T(i, j, k) + T(i, j - 1, k)) * std::cos(YV(j - 1)) * lm;
+                a(5, i, j, k) = c * (T(i, j + 1, k) + T(i, j, k)) * std::cos(YV(j)) * lm;
+                a(2, i, j, k) = c * (T(i, j + 1, k) + T(i, j, k)) * std::cos(YV(j)) * lm;
+            }
+            break;
+        case 5:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double c = 1.0 / (4 * std::cos(Y(j)) * dy), lm = double(1 - LM(i, j, l));
+                a(4, i, j, k) = -(V(i, j - 1, k) + V(i - 1, j - 1, k)) * c * std::cos(YV(j - 1)) * lm;
+                a(6, i, j, k) = (V(i, j, k) + V(i - 1, j, k)) * c * std::cos(YV(j)) * lm;
+                a(5, i, j, k) = a(4, i, j, k) + a(6, i, j, k);
+            }
+            break;
+        case 6: {
+            double tdzi = 1.0 / (2 * dz);
+            for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double lm = double(1 - LM(i, j, l));
+                for (int k = 1; k <= l - 1; ++k) {
+                    a(14, i, j, k) = -tdzi * lm * (T(i, j, k) + T(i, j, k - 1)) / DFZT(k);
+                    a(5, i, j, k) = tdzi * lm * (T(i, j, k + 1) + T(i, j, k)) / DFZT(k);
+                }
+                int k = l;
+                a(14, i, j, k) = -tdzi * lm * (T(i, j, k) + T(i, j, k - 1)) / DFZT(k);
+                a(5, i, j, k) = 0.0;
+            }
+        } break;
+        case 7: {
+            double tdzi = 1.0 / (2 * dz);
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                double lm = double(1 - LM(i, j, l));
+                a(14, i, j, k) = -W(i, j, k - 1) * lm * tdzi / DFZT(k);
+                a(23, i, j, k) = W(i, j, k) * lm * tdzi / DFZT(k);
+                a(5, i, j, k) = a(14, i, j, k) + a(23, i, j, k);
+            }
+        } break;
+        }
+    }
+    // ---- wnlin: src/ocean/spf.F90:486-542 ----
+    void wnlin(int type, Atom& a, Arr3& T) {
+        a.zero();
+        for (int k = 1; k <= l - 1; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            double t0 = T(i, j, k), t1 = T(i, j, k + 1);
+            switch (type) {
+            case 1: a(23, i, j, k) = (t0 + t1) / 2.; a(5, i, j, k) = (t0 + t1) / 2.; break;
+            case 2: a(23, i, j, k) = t1 / 4.; a(5, i, j, k) = (t0 + 2 * t1) / 4.; break;
+            case 3: {
+                double q = t0 + t1;
+                a(5, i, j, k) = 0.375 * (q * q);
+                a(23, i, j, k) = 0.375 * (q * q);
+            } break;
+            case 4:
+                a(5, i, j, k) = 0.125 * (t0 * t0 + 3 * t1 * t0 + 3 * t1 * t1);
+                a(23, i, j, k) = 0.125 * t1 * t1;
+                break;
+            }
+        }
+    }
+    // ---- unlin: src/ocean/spf.F90:544-665 ----
+    void unlin(int type, Atom& a, Arr3& U, Arr3& V, Arr3& W) {
+        a.zero();
+        switch (type) {
+        case 1:
+        case 2: {
+            double f = (type == 2) ? 2.0 : 1.0;
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) {
+                double c = 1.0 / (2 * std::cos(YV(j)) * dx);
+                for (int i = 1; i <= n - 1; ++i) a(8, i, j, k) = (type == 2 ? f * U(i + 1, j, k) : U(i + 1, j, k)) * c;
+                for (int i = 2; i <= n; ++i) a(2, i, j, k) = -(type == 2 ? f * U(i - 1, j, k) : U(i - 1, j, k)) * c;
+            }
+        } break;
+        case 3:
+        case 4: {
+            Arr3& Q = (type == 3) ? V : U;
+            for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) {
+                for (int j = 2; j <= m; ++j) {
+                    double c = 1.0 / (2 * std::cos(YV(j)) * dy);
+                    a(4, i, j, k) = -Q(i, j - 1, k) * std::cos(YV(j - 1)) * c;
+                }
+                for (int j = 1; j <= m - 1; ++j) {
+                    double c = 1.0 / (2 * std::cos(YV(j)) * dy);
+                    a(6, i, j, k) = Q(i, j + 1, k) * std::cos(YV(j + 1)) * c;
+                }
+            }
+        } break;
+        case 5:
+            for (int k = 1; k <= l; ++k) {
+                double tdzi = 1.0 / (8 * DFZT(k) * dz);
+                for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                    a(23, i, j, k) = (W(i, j, k) + W(i, j + 1, k) + W(i + 1, j, k) + W(i + 1, j + 1, k)) * tdzi;
+                    a(14, i, j, k) = -(W(i, j, k - 1) + W(i, j + 1, k - 1) + W(i + 1, j, k - 1) + W(i + 1, j + 1, k - 1)) * tdzi;
+                    a(5, i, j, k) = a(14, i, j, k) + a(23, i, j, k);
+                }
+            }
+            break;
+        case 6:
+            for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) for (int k = 1; k <= l; ++k) {
+                double tdzi = 1.0 / (8 * DFZT(k) * dz);
+                double up = (U(i, j, k) + U(i, j, k + 1)) * tdzi;
+                double dn = -(U(i, j, k) + U(i, j, k - 1)) * tdzi;
+                a(5, i, j, k) = up; a(6, i, j, k) = up; a(8, i, j, k) = up; a(9, i, j, k) = up;
+                a(14, i, j, k) = dn; a(15, i, j, k) = dn; a(17, i, j, k) = dn; a(18, i, j, k) = dn;
+            }
+            break;
+        case 7:
+        case 8: {
+            Arr3& Q = (type == 7) ? V : U;
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+                a(5, i, j, k) = Q(i, j, k) * std::tan(YV(j));
+        } break;
+        }
+    }
+    // ---- vnlin: src/ocean/spf.F90:667-790 ----
+    void vnlin(int type, Atom& a, Arr3& U, Arr3& V, Arr3& W) {
+        a.zero();
+        switch (type) {
+        case 1:
+        case 2: {
+            Arr3& Q = (type == 1) ? U : V;
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) {
+                double c = 1.0 / (2 * std::cos(YV(j)) * dx);
+                for (int i = 1; i <= n - 1; ++i) a(8, i, j, k) = Q(i + 1, j, k) * c;
+                for (int i = 2; i <= n; ++i) a(2, i, j, k) = -Q(i - 1, j, k) * c;
+            }
+        } break;
+        case 3:
+        case 4: {
+            for (int k = 1; k <= l; ++k) for (int i = 1; i <= n; ++i) {
+                for (int j = 1; j <= m - 1; ++j) {
+                    double c = 1.0 / (2 * std::cos(YV(j)) * dy);
+                    a(6, i, j, k) = (type == 4 ? 2 * V(i, j + 1, k) : V(i, j + 1, k)) * std::cos(YV(j + 1)) * c;
+                }
+                for (int j = 2; j <= m; ++j) {
+                    double c = 1.0 / (2 * std::cos(YV(j)) * dy);
+                    a(4, i, j, k) = -(type == 4 ? 2 * V(i, j - 1, k) : V(i, j - 1, k)) * std::cos(YV(j - 1)) * c;
+                }
+            }
+        } break;
+        case 5:
+            unlin(5, a, U, V, W);
+            break;
+        case 6:
+            unlin(6, a, V, V, W);
+            break;
+        case 7:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+                a(5, i, j, k) = U(i, j, k) * std::tan(YV(j));
+            break;
+        case 8:
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+                a(5, i, j, k) = 2 * U(i, j, k) * std::tan(YV(j));
+            break;
+        }
+    }
+
+    // ---- nlin_rhs: src/ocean/usrc.F90:792-887 ----
+    void nlin_rhs(const double* un) {
+        double lambda = par[LAMB], epsr = par[ROSB], Ra = par[RAYL], xes = par[NLES];
+        (void)lambda;
+        usol(un);
+        Atom a1 = mk(), a2 = mk(), a3 = mk(), a4 = mk();
+        unlin(1, a1, u, v, w); unlin(3, a2, u, v, w); unlin(5, a3, u, v, w); unlin(7, a4, u, v, w);
+        addAn(UU, UU, [&](double r, int kk, int i, int j, int k) {
+            return r + epsr * (a1(kk, i, j, k) + a2(kk, i, j, k) + a3(kk, i, j, k) + a4(kk, i, j, k));
+        });
+        vnlin(1, a1, u, v, w); vnlin(3, a2, u, v, w); vnlin(5, a3, u, v, w); vnlin(7, a4, u, v, w);
+        addAn(VV, UU, [&](double r, int kk, int i, int j, int k) { return r + epsr * a4(kk, i, j, k); });
+        addAn(VV, VV, [&](double r, int kk, int i, int j, int k) {
+            return r + epsr * (a1(kk, i, j, k) + a2(kk, i, j, k) + a3(kk, i, j, k));
+        });
+        wnlin(2, a1, t); wnlin(4, a2, t);
+        addAn(WW, TT, [&](double r, int kk, int i, int j, int k) {
+            return r - Ra * xes * alpt2 * a1(kk, i, j, k) + Ra * xes * alpt3 * a2(kk, i, j, k);
+        });
+        tnlin(3, a1, u, v, w, t); tnlin(5, a2, u, v, w, t); tnlin(7, a3, u, v, w, t);
+        addAn(TT, TT, [&](double r, int kk, int i, int j, int k) {
+            return r + a1(kk, i, j, k) + a2(kk, i, j, k) + a3(kk, i, j, k);
+        });
+        tnlin(3, a1, u, v, w, s); tnlin(5, a2, u, v, w, s); tnlin(7, a3, u, v, w, s);
+        addAn(SS, SS, [&](double r, int kk, int i, int j, int k) {
+            return r + a1(kk, i, j, k) + a2(kk, i, j, k) + a3(kk, i, j, k);
+        });
+    }
+
+    // ---- nlin_jac: src/ocean/usrc.F90:890-1012 ----
+    void nlin_jac(const double* un) {
+        double epsr = par[ROSB], Ra = par[RAYL], xes = par[NLES];
+        usol(un);
+        Atom a1 = mk(), a2 = mk(), a3 = mk(), a4 = mk(), a5 = mk(), a6 = mk(), a7 = mk();
+        // u-equation
+        unlin(2, a1, u, v, w); unlin(3, a2, u, v, w); unlin(4, a3, u, v, w); unlin(5, a4, u, v, w);
+        unlin(6, a5, u, v, w); unlin(7, a6, u, v, w); unlin(8, a7, u, v, w);
+        addAn(UU, UU, [&](double r, int kk, int i, int j, int k) {
+            return r + epsr * (a1(kk, i, j, k) + a2(kk, i, j, k) + a4(kk, i, j, k) + a6(kk, i, j, k));
+        });
+        addAn(UU, VV, [&](double r, int kk, int i, int j, int k) { return r + epsr * (a3(kk, i, j, k) + a7(kk, i, j, k)); });
+        addAn(UU, WW, [&](double r, int kk, int i, int j, int k) { return r + epsr * a5(kk, i, j, k); });
+        // v-equation
+        vnlin(1, a1, u, v, w); vnlin(2, a2, u, v, w); vnlin(4, a3, u, v, w); vnlin(5, a4, u, v, w);
+        vnlin(6, a5, u, v, w); vnlin(8, a6, u, v, w);
+        addAn(VV, UU, [&](double r, int kk, int i, int j, int k) { return r + epsr * (a6(kk, i, j, k) + a2(kk, i, j, k)); });
+        addAn(VV, VV, [&](double r, int kk, int i, int j, int k) {
+            return r + epsr * (a1(kk, i, j, k) + a3(kk, i, j, k) + a4(kk, i, j, k));
+        });
+        addAn(VV, WW, [&](double r, int kk, int i, int j, int k) { return r + epsr * a5(kk, i, j, k); });
+        // w-equation
+        wnlin(1, a1, t); wnlin(3, a2, t);
+        addAn(WW, TT, [&](double r, int kk, int i, int j, int k) {
+            return r - Ra * xes * alpt2 * a1(kk, i, j, k) + Ra * xes * alpt3 * a2(kk, i, j, k);
+        });
+        // T and S equations
+        for (int q = 0; q < 2; ++q) {
+            Arr3& X = q == 0 ? t : s;
+            int A = q == 0 ? TT : SS;
+            tnlin(2, a1, u, v, w, X); tnlin(3, a2, u, v, w, X); tnlin(4, a3, u, v, w, X);
+            tnlin(5, a4, u, v, w, X); tnlin(6, a5, u, v, w, X); tnlin(7, a6, u, v, w, X);
+            addAn(A, UU, [&](double r, int kk, int i, int j, int k) { return r + a1(kk, i, j, k); });
+            addAn(A, VV, [&](double r, int kk, int i, int j, int k) { return r + a3(kk, i, j, k); });
+            addAn(A, WW, [&](double r, int kk, int i, int j, int k) { return r + a5(kk, i, j, k); });
+            addAn(A, A, [&](double r, int kk, int i, int j, int k) {
+                return r + a2(kk, i, j, k) + a4(kk, i, j, k) + a6(kk, i, j, k);
+            });
+        }
+    }
+
+    // ---- boundaries: src/ocean/boundary.F90:2-393 ----
+    void boundaries() {
+        auto A = [&](int kk, int a, int b, int i, int j, int k) -> double& { return AN(kk, a, b, i, j, k); };
+        auto zeroPos = [&](int kk, int i, int j, int k) {
+            for (int b = 1; b <= NUN; ++b) for (int a = 1; a <= NUN; ++a) A(kk, a, b, i, j, k) = 0.0;
+        };
+        auto zeroPosCol = [&](int kk, int b, int i, int j, int k) {
+            for (int a = 1; a <= NUN; ++a) A(kk, a, b, i, j, k) = 0.0;
+        };
+        auto foldCol = [&](int dst, int src, int b, int i, int j, int k) {
+            for (int a = 1; a <= NUN; ++a) A(dst, a, b, i, j, k) = A(dst, a, b, i, j, k) + A(src, a, b, i, j, k);
+        };
+        auto dirRow = [&](int a, int i, int j, int k) {   // An(:,a,:) = 0; An(5,:,a) = 0; An(5,a,a) = 1
+            for (int b = 1; b <= NUN; ++b) for (int kk = 1; kk <= NP; ++kk) A(kk, a, b, i, j, k) = 0.0;
+            zeroPosCol(5, a, i, j, k);
+            A(5, a, a, i, j, k) = 1.0;
+        };
+        for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) for (int k = 1; k <= l; ++k) {
+            int southw = LM(i - 1, j - 1, k), west = LM(i - 1, j, k), nwest = LM(i - 1, j + 1, k);
+            int south = LM(i, j - 1, k), center = LM(i, j, k), north = LM(i, j + 1, k);
+            int southe = LM(i + 1, j - 1, k), east = LM(i + 1, j, k), neast = LM(i + 1, j + 1, k);
+            int southwb = LM(i - 1, j - 1, k - 1), westb = LM(i - 1, j, k - 1), nwestb = LM(i - 1, j + 1, k - 1);
+            int southb = LM(i, j - 1, k - 1), bottom = LM(i, j, k - 1), northb = LM(i, j + 1, k - 1);
+            int southeb = LM(i + 1, j - 1, k - 1), eastb = LM(i + 1, j, k - 1), neastb = LM(i + 1, j + 1, k - 1);
+            int southwt = LM(i - 1, j - 1, k + 1), westt = LM(i - 1, j, k + 1), nwestt = LM(i - 1, j + 1, k + 1);
+            int southt = LM(i, j - 1, k + 1), top = LM(i, j, k + 1), northt = LM(i, j + 1, k + 1);
+            int southet = LM(i + 1, j - 1, k + 1), eastt = LM(i + 1, j, k + 1), neastt = LM(i + 1, j + 1, k + 1);
+            int southee = -1, easteast = -1, northee = -1, nnorthee = -1, nnwest = -1, nnorth = -1, nneast = -1;
+            if (i < n) {
+                southee = LM(i + 2, j - 1, k);
+                easteast = LM(i + 2, j, k);
+                northee = LM(i + 2, j + 1, k);
+                if (j < m) nnorthee = LM(i + 2, j + 2, k);
+            }
+            if (j < m) { nnwest = LM(i, j + 2, k); nnorth = LM(i, j + 2, k); nneast = LM(i, j + 2, k); }
+
+            if (center == OCEAN) {
+                if (bottom == LAND) {
+                    if (westb == LAND && southwb == LAND && southb == LAND) { foldCol(1, 10, UU, i, j, k); foldCol(1, 10, VV, i, j, k); }
+                    zeroPosCol(10, UU, i, j, k); zeroPosCol(10, VV, i, j, k);
+                    if (westb == LAND && neastb == LAND && northb == LAND) { foldCol(2, 11, UU, i, j, k); foldCol(2, 11, VV, i, j, k); }
+                    zeroPosCol(11, UU, i, j, k); zeroPosCol(11, VV, i, j, k);
+                    if (eastb == LAND && southeb == LAND && southb == LAND) { foldCol(4, 13, UU, i, j, k); foldCol(4, 13, VV, i, j, k); }
+                    zeroPosCol(13, UU, i, j, k); zeroPosCol(13, VV, i, j, k);
+                    if (eastb == LAND && neastb == LAND && northb == LAND) { foldCol(5, 14, UU, i, j, k); foldCol(5, 14, VV, i, j, k); }
+                    foldCol(5, 14, TT, i, j, k); foldCol(5, 14, SS, i, j, k);
+                    zeroPos(14, i, j, k);
+                }
+                if (southwb == LAND) zeroPos(10, i, j, k);
+                if (westb == LAND) zeroPos(11, i, j, k);
+                if (nwestb == LAND) zeroPos(12, i, j, k);
+                if (southb == LAND) zeroPos(13, i, j, k);
+                if (northb == LAND) zeroPos(15, i, j, k);
+                if (southeb == LAND) zeroPos(16, i, j, k);
+                if (eastb == LAND) zeroPos(17, i, j, k);
+                if (neastb == LAND) zeroPos(18, i, j, k);
+                if (top == LAND) {
+                    if (westt == LAND && southwt == LAND && southt == LAND) { foldCol(1, 19, UU, i, j, k); foldCol(1, 19, VV, i, j, k); }
+                    zeroPosCol(19, UU, i, j, k); zeroPosCol(19, VV, i, j, k);
+                    if (westt == LAND && nwestt == LAND && northt == LAND) { foldCol(2, 20, UU, i, j, k); foldCol(2, 20, VV, i, j, k); }
+                    zeroPosCol(20, UU, i, j, k); zeroPosCol(20, VV, i, j, k);
+                    if (eastt == LAND && southet == LAND && southt == LAND) { foldCol(4, 22, UU, i, j, k); foldCol(4, 22, VV, i, j, k); }
+                    zeroPosCol(22, UU, i, j, k); zeroPosCol(22, VV, i, j, k);
+                    if (eastt == LAND && neastt == LAND && northt == LAND) { foldCol(5, 23, UU, i, j, k); foldCol(5, 23, VV, i, j, k); }
+                    foldCol(5, 23, TT, i, j, k); foldCol(5, 23, SS, i, j, k);
+                    zeroPos(23, i, j, k);
+                    Frc[find_row2(i, j, k, WW) - 1] = 0.0;
+                    for (int b = 1; b <= NUN; ++b) for (int kk = 1; kk <= NP; ++kk) A(kk, WW, b, i, j, k) = 0.0;
+                    for (int a = 1; a <= NUN; ++a) {
+                        A(5, a, WW, i, j, k) = 1.0e-10; A(6, a, WW, i, j, k) = 1.0e-10;
+                        A(8, a, WW, i, j, k) = 1.0e-10; A(9, a, WW, i, j, k) = 1.0e-10;
+                    }
+                    A(5, WW, WW, i, j, k) = 1.0;
+                }
+                if (southwt == LAND) zeroPos(19, i, j, k);
+                if (westt == LAND) zeroPos(20, i, j, k);
+                if (nwestt == LAND) zeroPos(21, i, j, k);
+                if (southt == LAND) zeroPos(22, i, j, k);
+                if (northt == LAND) zeroPos(24, i, j, k);
+                if (southet == LAND) zeroPos(25, i, j, k);
+                if (eastt == LAND) zeroPos(26, i, j, k);
+                if (neastt == LAND) zeroPos(27, i, j, k);
+                if (southw == LAND) { zeroPosCol(1, UU, i, j, k); zeroPosCol(1, VV, i, j, k); }
+                if (west == LAND) {
+                    foldCol(5, 2, TT, i, j, k); foldCol(5, 2, SS, i, j, k);
+                    zeroPos(2, i, j, k);
+                    zeroPosCol(1, UU, i, j, k); zeroPosCol(1, VV, i, j, k);
+                }
+                if (nwest == LAND) {
+                    zeroPosCol(2, UU, i, j, k); zeroPosCol(2, VV, i, j, k);
+                    zeroPosCol(3, UU, i, j, k); zeroPosCol(3, VV, i, j, k);
+                } else if (j < m) {
+                    if (nnwest == LAND) { zeroPosCol(3, UU, i, j, k); zeroPosCol(3, VV, i, j, k); }
+                }
+                if (south == LAND) {
+                    foldCol(5, 4, SS, i, j, k); foldCol(5, 4, TT, i, j, k);
+                    zeroPos(4, i, j, k);
+                    zeroPosCol(1, UU, i, j, k); zeroPosCol(1, VV, i, j, k);
+                }
+                if (north == LAND) {
+                    zeroPosCol(2, UU, i, j, k); zeroPosCol(2, VV, i, j, k);
+                    A(2, PP, UU, i, j, k) = 0.0; A(2, PP, VV, i, j, k) = 0.0;
+                    A(5, PP, UU, i, j, k) = 0.0; A(5, PP, VV, i, j, k) = 0.0;
+                    Frc[find_row2(i, j, k, VV) - 1] = 0.0;
+                    dirRow(VV, i, j, k);
+                    Frc[find_row2(i, j, k, UU) - 1] = 0.0;
+                    dirRow(UU, i, j, k);
+                    foldCol(5, 6, SS, i, j, k); foldCol(5, 6, TT, i, j, k);
+                    zeroPos(6, i, j, k);
+                } else if (j < m) {
+                    if (nnorth == LAND) {
+                        zeroPosCol(3, UU, i, j, k); zeroPosCol(3, VV, i, j, k);
+                        zeroPosCol(6, UU, i, j, k); zeroPosCol(6, VV, i, j, k);
+                    }
+                }
+                if (southe == LAND) {
+                    zeroPosCol(4, UU, i, j, k); zeroPosCol(4, VV, i, j, k);
+                    zeroPosCol(7, UU, i, j, k); zeroPosCol(7, VV, i, j, k);
+                } else if (i < n) {
+                    if (southee == LAND) { zeroPosCol(7, UU, i, j, k); zeroPosCol(7, VV, i, j, k); }
+                }
+                if (east == LAND) {
+                    zeroPosCol(4, UU, i, j, k); zeroPosCol(4, VV, i, j, k);
+                    A(4, PP, UU, i, j, k) = 0.0; A(4, PP, VV, i, j, k) = 0.0;
+                    A(5, PP, UU, i, j, k) = 0.0; A(5, PP, VV, i, j, k) = 0.0;
+                    Frc[find_row2(i, j, k, UU) - 1] = 0.0;
+                    dirRow(UU, i, j, k);
+                    Frc[find_row2(i, j, k, VV) - 1] = 0.0;
+                    dirRow(VV, i, j, k);
+                    foldCol(5, 8, SS, i, j, k); foldCol(5, 8, TT, i, j, k);
+                    zeroPos(8, i, j, k);
+                    zeroPosCol(7, UU, i, j, k); zeroPosCol(7, VV, i, j, k);
+                } else if (i < n) {
+                    if (easteast == LAND) {
+                        zeroPosCol(7, UU, i, j, k); zeroPosCol(7, VV, i, j, k);
+                        zeroPosCol(8, UU, i, j, k); zeroPosCol(8, VV, i, j, k);
+                    }
+                }
+                if (neast == LAND) {
+                    Frc[find_row2(i, j, k, UU) - 1] = 0.0;
+                    dirRow(UU, i, j, k);
+                    Frc[find_row2(i, j, k, VV) - 1] = 0.0;
+                    dirRow(VV, i, j, k);
+                    zeroPosCol(7, UU, i, j, k); zeroPosCol(7, VV, i, j, k);
+                } else if (i < n || j < m) {
+                    if (i < n) {
+                        if (northee == LAND) {
+                            zeroPosCol(8, UU, i, j, k); zeroPosCol(8, VV, i, j, k);
+                            zeroPosCol(9, UU, i, j, k); zeroPosCol(9, VV, i, j, k);
+                        } else if (j < m) {
+                            if (nnorthee == LAND) { zeroPosCol(9, UU, i, j, k); zeroPosCol(9, VV, i, j, k); }
+                        }
+                    }
+                    if (j < m) {
+                        if (nneast == LAND) {
+                            zeroPosCol(6, UU, i, j, k); zeroPosCol(6, VV, i, j, k);
+                            zeroPosCol(9, UU, i, j, k); zeroPosCol(9, VV, i, j, k);
+                        }
+                    }
+                }
+            } else {
+                for (int b = 1; b <= NUN; ++b) for (int a = 1; a <= NUN; ++a) for (int kk = 1; kk <= NP; ++kk)
+                    A(kk, a, b, i, j, k) = 0.0;
+                for (int ii = 1; ii <= NUN; ++ii) {
+                    Frc[find_row2(i, j, k, ii) - 1] = 0.0;
+                    A(5, ii, ii, i, j, k) = 1.0;
+                }
+            }
+        }
+    }
+
+    // ---- shift: src/ocean/assemble.F90:142-179 ----
+    void shift(int i, int j, int k, int& i2, int& j2, int& k2, int kk) const {
+        if (kk < 10) { k2 = k; j2 = j - 1 + (kk + 2) % 3; i2 = i - 1 + (kk - 1) / 3; }
+        else if (kk < 19) { k2 = k - 1; j2 = j - 1 + (kk + 2) % 3; i2 = i - 1 + (kk - 10) / 3; }
+        else { k2 = k + 1; j2 = j - 1 + (kk + 2) % 3; i2 = i - 1 + (kk - 19) / 3; }
+        if (periodic) {
+            if (i2 == 0) i2 = n;
+            else if (i2 == n + 1) i2 = 1;
+        }
+    }
+    // ---- fillcolA: src/ocean/assemble.F90:57-139 (drop rule abs(c) > 1e-10) ----
+    std::vector<char> inDomain;   // per Fortran entry: neighbour inside 1..n,1..m,1..l
+    void fillcolA() {
+        begA.assign(ndim + 1, 0);
+        jcoA.clear(); coA.clear(); inDomain.clear();
+        int v = 1, row = 1;
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+            for (int ii = 1; ii <= NUN; ++ii) {
+                begA[row - 1] = v;
+                for (int kk = 1; kk <= NP; ++kk) for (int jj = 1; jj <= NUN; ++jj) {
+                    double c = AN(kk, ii, jj, i, j, k);
+                    if (std::fabs(c) > 1.0e-10) {
+                        coA.push_back(c);
+                        int i2, j2, k2;
+                        shift(i, j, k, i2, j2, k2, kk);
+                        jcoA.push_back(find_row2(i2, j2, k2, jj));
+                        inDomain.push_back(i2 >= 1 && i2 <= n && j2 >= 1 && j2 <= m && k2 >= 1 && k2 <= l);
+                        ++v;
+                    }
+                }
+                ++row;
+            }
+        begA[ndim] = v;
+    }
+    // ---- fillcolB: src/ocean/assemble.F90:18-54 ----
+    void fillcolB() {
+        coB.assign(ndim, 0.0);
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+            if (LM(i, j, k) == OCEAN) {
+                if (LM(i + 1, j, k) != LAND) coB[find_row2(i, j, k, UU) - 1] = -par[ROSB];
+                if (LM(i, j + 1, k) != LAND) coB[find_row2(i, j, k, VV) - 1] = -par[ROSB];
+                coB[find_row2(i, j, k, TT) - 1] = -1.0;
+                coB[find_row2(i, j, k, SS) - 1] = -1.0;
+            }
+    }
+    // ---- matAvec: src/ocean/matetc.F90:147-166 ----
+    void matAvec(const double* v1, double* v2) const {
+        for (int i = 0; i < ndim; ++i) {
+            double acc = 0.0;
+            for (int q = begA[i]; q < begA[i + 1]; ++q) acc = coA[q - 1] * v1[jcoA[q - 1] - 1] + acc;
+            v2[i] = acc;
+        }
+    }
+
+    // ---- rhs: src/ocean/usrc.F90:523-603, sign flip of THCM.C:1008-1011 ----
+    void rhs(const double* un, double* F) {
+        An = Al;
+        nlin_rhs(un);
+        boundaries();
+        fillcolA();
+        std::vector<double> Au(ndim);
+        matAvec(un, Au.data());
+        for (int r = 0; r < ndim; ++r) {
+            double B = -Au[r] - 0.0 + Frc[r] - 0.0 * (1 - par[RESC]) * 0.0;
+            F[r] = B;
+        }
+        for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) for (int k = 1; k <= l; ++k)
+            for (int k1 = 1; k1 <= NUN; ++k1) {
+                int row = find_row2(i, j, k, k1) - 1;
+                F[row] = F[row] * double(1 - LM(i, j, k));
+            }
+        for (int r = 0; r < ndim; ++r) F[r] = -F[r];   // Epetra Scale(-1.0)
+    }
+    void assemble_rhs_matrix(const double* un) {
+        An = Al;
+        nlin_rhs(un);
+        boundaries();
+        fillcolA();
+    }
+    // ---- matrix: src/ocean/usrc.F90:449-521 ----
+    void matrix(const double* un) {
+        An = Al;
+        fillcolB();
+        nlin_jac(un);
+        boundaries();
+        fillcolA();
+    }
+
+    // ---- CreateMaximalGraph: src/ocean/THCM.C:2300-2580 (SRES = 1 path) ----
+    void build_graph() {
+        g_ptr.assign(ndim + 1, 0);
+        g_col.clear();
+        const int N = n, M = m, L = l;
+        auto fr = [&](int i, int j, int k, int xx) { return NUN * (k * N * M + N * j + i) + xx - 1; };
+        std::vector<int> idx;
+        auto ins = [&](int i, int j, int k, int xx) {
+            int ii = i;
+            if (periodic) ii = ((i % N) + N) % N;
+            if (ii >= 0 && j >= 0 && k >= 0 && ii < N && j < M && k < L) idx.push_back(fr(ii, j, k, xx));
+        };
+        std::vector<std::vector<int>> rows(ndim);
+        for (int k = 0; k < L; ++k) for (int j = 0; j < M; ++j) for (int i = 0; i < N; ++i) {
+            int g0 = fr(i, j, k, UU) - 0;   // row of UU (0-based)
+            idx.clear();
+            ins(i, j, k, UU); ins(i - 1, j, k, UU); ins(i + 1, j, k, UU); ins(i, j - 1, k, UU); ins(i, j + 1, k, UU);
+            ins(i, j, k - 1, UU); ins(i, j, k + 1, UU);
+            ins(i, j, k, VV); ins(i - 1, j, k, VV); ins(i + 1, j, k, VV); ins(i, j - 1, k, VV); ins(i, j + 1, k, VV);
+            ins(i, j, k, WW); ins(i + 1, j, k, WW); ins(i + 1, j + 1, k, WW); ins(i, j + 1, k, WW);
+            ins(i, j, k - 1, WW); ins(i + 1, j, k - 1, WW); ins(i + 1, j + 1, k - 1, WW); ins(i, j + 1, k - 1, WW);
+            ins(i, j, k, PP); ins(i + 1, j, k, PP); ins(i, j + 1, k, PP); ins(i + 1, j + 1, k, PP);
+            rows[g0 + 0] = idx;
+            idx.clear();
+            ins(i, j, k, VV); ins(i - 1, j, k, VV); ins(i + 1, j, k, VV); ins(i, j - 1, k, VV); ins(i, j + 1, k, VV);
+            ins(i, j, k - 1, VV); ins(i, j, k + 1, VV);
+            ins(i, j, k, UU); ins(i - 1, j, k, UU); ins(i + 1, j, k, UU);
+            ins(i, j, k, WW); ins(i + 1, j, k, WW); ins(i + 1, j + 1, k, WW); ins(i, j + 1, k, WW);
+            ins(i, j, k - 1, WW); ins(i + 1, j, k - 1, WW); ins(i + 1, j + 1, k - 1, WW); ins(i, j + 1, k - 1, WW);
+            ins(i, j, k, PP); ins(i + 1, j, k, PP); ins(i, j + 1, k, PP); ins(i + 1, j + 1, k, PP);
+            rows[g0 + 1] = idx;
+            idx.clear();
+            ins(i, j, k, WW); ins(i, j, k, PP); ins(i, j, k + 1, PP); ins(i, j, k, TT); ins(i, j, k + 1, TT);
+            ins(i, j, k, SS); ins(i, j, k + 1, SS);
+            rows[g0 + 2] = idx;
+            idx.clear();
+            ins(i, j, k, PP);
+            ins(i, j, k, UU); ins(i - 1, j, k, UU); ins(i, j - 1, k, UU); ins(i - 1, j - 1, k, UU);
+            ins(i, j, k, VV); ins(i - 1, j, k, VV); ins(i, j - 1, k, VV); ins(i - 1, j - 1, k, VV);
+            ins(i, j, k, WW); ins(i, j, k - 1, WW);
+            rows[g0 + 3] = idx;
+            for (int q = 0; q < 2; ++q) {
+                int A = q == 0 ? TT : SS, O = q == 0 ? SS : TT;
+                idx.clear();
+                ins(i, j, k, A); ins(i - 1, j, k, A); ins(i + 1, j, k, A); ins(i, j - 1, k, A); ins(i, j + 1, k, A);
+                ins(i, j, k - 1, A); ins(i, j, k + 1, A);
+                ins(i, j, k, UU); ins(i - 1, j, k, UU); ins(i - 1, j - 1, k, UU); ins(i, j - 1, k, UU);
+                ins(i, j, k, VV); ins(i - 1, j, k, VV); ins(i - 1, j - 1, k, VV); ins(i, j - 1, k, VV);
+                ins(i, j, k, WW); ins(i, j, k - 1, WW);
+                ins(i, j, k, O); ins(i, j, k - 1, O); ins(i, j, k + 1, O);
+                rows[g0 + 4 + q] = idx;
+            }
+        }
+        for (int r = 0; r < ndim; ++r) {
+            auto& rr = rows[r];
+            std::sort(rr.begin(), rr.end());
+            rr.erase(std::unique(rr.begin(), rr.end()), rr.end());   // Epetra merges duplicates
+            g_ptr[r + 1] = g_ptr[r] + int(rr.size());
+            g_col.insert(g_col.end(), rr.begin(), rr.end());
+        }
+    }
+    // Scatter of THCM::evaluate (src/ocean/THCM.C:1082-1162): ReplaceGlobalValues
+    // into the zeroed maximal-graph matrix, entry by entry in Fortran order.
+    int scatter(double* values) const {
+        std::fill(values, values + g_col.size(), 0.0);
+        int excluded = 0;
+        for (int r = 0; r < ndim; ++r) {
+            const int* b = g_col.data() + g_ptr[r];
+            const int* e = g_col.data() + g_ptr[r + 1];
+            for (int q = begA[r]; q < begA[r + 1]; ++q) {
+                int col = jcoA[q - 1] - 1;
+                const int* f = std::lower_bound(b, e, col);
+                if (f != e && *f == col) values[g_ptr[r] + (f - b)] = coA[q - 1];
+                else ++excluded;
+            }
+        }
+        return excluded;
+    }
+
+    // ---- compute_psim: src/ocean/thcm_utils.F90:95-118, OceanGrid.C:270-330 ----
+    void psim(const double* un, double* out) {
+        usol(un);
+        std::vector<double> vs((m + 1) * l);
+        for (int k = 1; k <= l; ++k) for (int j = 0; j <= m; ++j) {
+            double sum = 0.0;
+            for (int i = 1; i <= n; ++i) sum += v(i, j, k);
+            vs[(m + 1) * (k - 1) + j] = sum * dx;
+        }
+        std::fill(out, out + (m + 1) * (l + 1), 0.0);
+        for (int j = 1; j <= m; ++j) {
+            double cs = std::cos(YV(j));
+            for (int k = 1; k <= l; ++k)
+                if (Z(k) * hdim < -500)
+                    out[(m + 1) * k + j] = -cs * vs[(m + 1) * (k - 1) + j] * dz * DFZT(k) + out[(m + 1) * (k - 1) + j];
+        }
+    }
+
+    // ---- init: src/ocean/usrc.F90:6-139 ----
+    void init(const iemic_oracle_config& c, const int* lm) {
+        n = c.n; m = c.m; l = c.l; ndim = n * m * l * NUN;
+        periodic = c.periodic != 0;
+        xmin = c.xmin_deg * PI / 180.0; xmax = c.xmax_deg * PI / 180.0;
+        ymin = c.ymin_deg * PI / 180.0; ymax = c.ymax_deg * PI / 180.0;
+        hdim = c.hdim; qz = c.qz; alphaT = c.alphaT; alphaS = c.alphaS;
+        ih = c.ih; coriolis_on = c.coriolis_on; TRES = c.tres; SRES = c.sres;
+        iza = c.iza; ite = c.ite; its = c.its; forcing_type = c.forcing_type;
+        landm.assign(size_t(n + 2) * (m + 2) * (l + 2), OCEAN);
+        if (lm) {
+            for (size_t q = 0; q < landm.size(); ++q) landm[q] = lm[q];
+        } else {   // Topography = 1: no continents (src/ocean/topo.F90 depth3land case 1)
+            std::fill(landm.begin(), landm.end(), LAND);
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) LM(i, j, k) = OCEAN;
+        }
+        for (int k = 0; k <= l + 1; ++k) for (int j = 0; j <= m + 1; ++j) for (int i = 0; i <= n + 1; ++i)
+            if (!periodic && LM(i, j, k) == PERIO) LM(i, j, k) = OCEAN;
+        if (!periodic)
+            for (int k = 0; k <= l + 1; ++k) for (int j = 0; j <= m + 1; ++j) { LM(0, j, k) = LAND; LM(n + 1, j, k) = LAND; }
+        for (int k = 0; k <= l + 1; ++k) for (int i = 0; i <= n + 1; ++i) { LM(i, 0, k) = LAND; LM(i, m + 1, k) = LAND; }
+        for (int j = 0; j <= m + 1; ++j) for (int i = 0; i <= n + 1; ++i) { LM(i, j, 0) = LAND; LM(i, j, l + 1) = LAND; }
+        size_t nm = size_t(n) * m;
+        taux.assign(nm, 0); tauy.assign(nm, 0); tatm.assign(nm, 0); emip.assign(nm, 0);
+        spert.assign(nm, double(SRES)); adapted_emip.assign(nm, 0);
+        internal_temp.assign(nm * l, 0); internal_salt.assign(nm * l, 0);
+        Frc.assign(ndim, 0.0);
+        Al.assign(size_t(NP) * NUN * NUN * n * m * l, 0.0);
+        An = Al;
+        grid();
+        double dzne = dz * DFZT(l);
+        QTnd = r0dim / (udim * cp0 * rhodim * hdim * dzne);
+        QSnd = s0 * r0dim / (deltas * udim * hdim * dzne);
+        stpnt();
+        forcing();
+        lin();
+        build_graph();
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_create(const iemic_oracle_config* cfg, const int* landm) {
+    Model* M = new Model();
+    M->init(*cfg, landm);
+    return M;
+}
+void oracle_destroy(void* h) { delete static_cast<Model*>(h); }
+int oracle_ndim(void* h) { return static_cast<Model*>(h)->ndim; }
+void oracle_get_landm(void* h, int* out) {
+    Model* M = static_cast<Model*>(h);
+    std::copy(M->landm.begin(), M->landm.end(), out);
+}
+void oracle_set_forcing(void* h, const double* taux, const double* tauy, const double* tatm,
+                        const double* emip, const double* spert) {
+    Model* M = static_cast<Model*>(h);
+    size_t nm = size_t(M->n) * M->m;
+    if (taux) std::copy(taux, taux + nm, M->taux.begin());
+    if (tauy) std::copy(tauy, tauy + nm, M->tauy.begin());
+    if (tatm) std::copy(tatm, tatm + nm, M->tatm.begin());
+    if (emip) std::copy(emip, emip + nm, M->emip.begin());
+    if (spert) std::copy(spert, spert + nm, M->spert.begin());
+    M->forcing();
+    M->lin();
+}
+void oracle_set_par(void* h, int idx, double value) {
+    Model* M = static_cast<Model*>(h);
+    if (idx >= 1 && idx <= NPAR) M->par[idx] = value;
+    M->forcing();
+    M->lin();
+}
+double oracle_get_par(void* h, int idx) {
+    Model* M = static_cast<Model*>(h);
+    return (idx >= 1 && idx <= NPAR) ? M->par[idx] : 0.0;
+}
+void oracle_get_frc(void* h, double* out) {
+    Model* M = static_cast<Model*>(h);
+    std::copy(M->Frc.begin(), M->Frc.end(), out);
+}
+void oracle_get_grid(void* h, double* x, double* y, double* xu, double* yv, double* z, double* zw,
+                     double* dfzT, double* dfzW) {
+    Model* M = static_cast<Model*>(h);
+    std::copy(M->x.begin(), M->x.end(), x);
+    std::copy(M->y.begin(), M->y.end(), y);
+    std::copy(M->xu.begin(), M->xu.end(), xu);
+    std::copy(M->yv.begin(), M->yv.end(), yv);
+    std::copy(M->z.begin(), M->z.end(), z);
+    std::copy(M->zw.begin(), M->zw.end(), zw);
+    std::copy(M->dfzT.begin(), M->dfzT.end(), dfzT);
+    std::copy(M->dfzW.begin(), M->dfzW.end(), dfzW);
+}
+void oracle_rhs(void* h, const double* x, double* F) {
+    Model* M = static_cast<Model*>(h);
+    // forcing() is re-run because boundaries() zeroes Frc entries in place,
+    // exactly like the reference, where Frc persists across calls.
+    M->rhs(x, F);
+}
+int oracle_fortran_nnz(void* h) { return int(static_cast<Model*>(h)->coA.size()); }
+void oracle_fortran_csr(void* h, int* beg, int* jco, double* co) {
+    Model* M = static_cast<Model*>(h);
+    std::copy(M->begA.begin(), M->begA.end(), beg);
+    std::copy(M->jcoA.begin(), M->jcoA.end(), jco);
+    std::copy(M->coA.begin(), M->coA.end(), co);
+}
+void oracle_assemble_rhs_matrix(void* h, const double* x) { static_cast<Model*>(h)->assemble_rhs_matrix(x); }
+int64_t oracle_graph_nnz(void* h) { return int64_t(static_cast<Model*>(h)->g_col.size()); }
+void oracle_graph(void* h, int* row_ptr, int* col_idx) {
+    Model* M = static_cast<Model*>(h);
+    std::copy(M->g_ptr.begin(), M->g_ptr.end(), row_ptr);
+    std::copy(M->g_col.begin(), M->g_col.end(), col_idx);
+}
+int oracle_jacobian(void* h, const double* x, double* values) {
+    Model* M = static_cast<Model*>(h);
+    M->matrix(x);
+    return M->scatter(values);
+}
+void oracle_mass(void* h, double* diagB) {
+    Model* M = static_cast<Model*>(h);
+    M->fillcolB();
+    std::copy(M->coB.begin(), M->coB.end(), diagB);
+}
+void oracle_psim(void* h, const double* x, double* psim) { static_cast<Model*>(h)->psim(x, psim); }
+double oracle_An(void* h, int kk, int A, int B, int i, int j, int k) {
+    return static_cast<Model*>(h)->AN(kk, A, B, i, j, k);
+}
+
+}  // extern "C"
