@@ -18,7 +18,9 @@ inline void ck(cudaError_t e) {
     if (e != cudaSuccess) throw EngineError(IEMIC_ERR_CUDA);
 }
 
-struct NdLu;   // nested-dissection block factorisation (ndlu.cu)
+struct NdLu;     // nested-dissection block factorisation (ndlu.cu)
+struct NdPlan;   // its symbolic analysis
+struct Krylov;   // Krylov workspace (krylov.cu)
 
 struct Engine {
     iemic_config cfg{};
@@ -49,12 +51,14 @@ struct Engine {
     float* d_val32 = nullptr;
 
     bool jac_valid = false;
-    bool fact_stale = true;
+    bool fact64_stale = true, fact32_stale = true;   // J changed since the last factorisation
 
     // solver state (krylov.cu / ndlu.cu)
+    NdPlan* ndplan = nullptr;
     NdLu* lu64 = nullptr;
     NdLu* lu32 = nullptr;
-    struct Krylov* kry = nullptr;
+    Krylov* kry = nullptr;
+    std::vector<int> h_col;   // host copy of the CSR column indices
 
     ~Engine();
     void init(const iemic_config& c, const int* landm_in);
@@ -75,7 +79,10 @@ struct Engine {
     void ensure_solver();
     void build_preconditioner(int precision);
     int solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);
+    int solve_transpose_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);
     void apply_precon(int precision, const double* v, double* out);
+    NdLu*& lu_for(int precision);
+    const std::vector<int>& host_col_idx();
 };
 
 }  // namespace iemic

@@ -1,11 +1,29 @@
-// Sparse matrix-vector products on the maximal-graph CSR (FP64 and FP32).
+// Krylov solvers of the Newton step: SpMV, right-preconditioned restarted
+// GMRES and FP64 iterative refinement around an FP32 GMRES.
 //
-// Rows hold 7..24 entries, so four lanes share a row: each lane walks every
-// fourth entry and the partial sums are reduced with warp shuffles. A warp
-// covers eight consecutive rows, so its loads of col_idx/values are
-// contiguous. The state vector is at most a few tens of MB and stays resident
-// in the 126 MB L2, so the gathers of x hit L2; DRAM traffic is the matrix.
+// The reference solves J x = b with Belos block GMRES (block size 1,
+// "Flexible Gmres", DGKS orthogonalisation, restart = "FGMRES iterations";
+// src/ocean/Ocean.C:971-1030). Here the preconditioner is fixed during a
+// solve, so right-preconditioned GMRES with x = x0 + M^{-1} V y gives the
+// same iterates as the flexible variant without storing the M^{-1} V basis.
+// Orthogonalisation is classical Gram-Schmidt applied twice (CGS2, the
+// DGKS-style reorthogonalisation). Each pass fuses the (j+1) dot products
+// into one sweep over the basis and the update into a second sweep. The
+// Hessenberg least-squares problem (Givens rotations) is solved in FP64.
+//
+// Mixed precision (IEMIC_PREC_MIXED): J, the factorisation, the Krylov basis
+// and all inner products are FP32. The residual r = b - J x, the solution
+// update and the convergence test stay FP64 (outer iterative refinement).
+//
+// SpMV: rows hold 7..24 entries, so four lanes share a row and reduce with
+// warp shuffles; a warp covers eight consecutive rows (contiguous loads of
+// col_idx/values). The state vectors stay resident in the 126 MB L2.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
 #include "engine.cuh"
+#include "ndlu.cuh"
 
 namespace iemic {
 namespace {
@@ -24,6 +42,113 @@ __global__ void __launch_bounds__(256) spmv_csr4(int nrows, const int* __restric
     }
 }
 
+// y = b - J x in FP64
+__global__ void __launch_bounds__(256) residual_csr4(int nrows, const int* __restrict__ rp, const int* __restrict__ ci,
+                                                     const double* __restrict__ v, const double* __restrict__ x,
+                                                     const double* __restrict__ b, double* __restrict__ y) {
+    const int lane = threadIdx.x & 3;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; row < nrows; row += (gridDim.x * blockDim.x) >> 2) {
+        const int s0 = __ldg(rp + row), e = __ldg(rp + row + 1);
+        double s = 0.0;
+        for (int q = s0 + lane; q < e; q += 4) s += __ldg(v + q) * __ldg(x + __ldg(ci + q));
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (lane == 0) y[row] = b[row] - s;
+    }
+}
+
+// partial sums of dots[i] = <V_i, w>, i < nv, per block (double partials)
+template <class T>
+__global__ void __launch_bounds__(256) multidot(int n, int nv, const T* __restrict__ V, const T* __restrict__ w,
+                                                double* __restrict__ part) {
+    constexpr int MAXV = 8;   // basis vectors per sweep chunk
+    __shared__ double red[MAXV][256 / 32];
+    for (int i0 = 0; i0 < nv; i0 += MAXV) {
+        const int cnt = min(MAXV, nv - i0);
+        T acc[MAXV];
+#pragma unroll
+        for (int q = 0; q < MAXV; ++q) acc[q] = T(0);
+        for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+            const T wr = w[r];
+#pragma unroll
+            for (int q = 0; q < MAXV; ++q)
+                if (q < cnt) acc[q] += V[size_t(i0 + q) * n + r] * wr;
+        }
+#pragma unroll
+        for (int q = 0; q < MAXV; ++q) {
+            double a = double(acc[q]);
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            double s = 0.0;
+            for (int q = 0; q < 256 / 32; ++q) s += red[threadIdx.x][q];
+            part[size_t(blockIdx.x) * nv + i0 + threadIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+// dots[i] = sum over blocks of the partials; also accumulates into h if given
+__global__ void reduce_parts(int nblocks, int nv, const double* __restrict__ part, double* __restrict__ dots,
+                             double* __restrict__ hacc, int first) {
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblocks; ++b) s += part[size_t(b) * nv + i];
+        dots[i] = s;
+        if (hacc) hacc[i] = first ? s : hacc[i] + s;
+    }
+}
+// w -= sum_i h[i] V_i
+template <class T>
+__global__ void __launch_bounds__(256) basis_update(int n, int nv, const T* __restrict__ V, const double* __restrict__ h,
+                                                    T* __restrict__ w) {
+    __shared__ T hs[1024];
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = T(h[i]);
+    __syncthreads();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        T s = w[r];
+        for (int i = 0; i < nv; ++i) s -= hs[i] * V[size_t(i) * n + r];
+        w[r] = s;
+    }
+}
+// y = sum_i c[i] V_i
+template <class T>
+__global__ void combine(int n, int nv, const T* __restrict__ V, const double* __restrict__ c, T* __restrict__ y) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int i = 0; i < nv; ++i) s += c[i] * double(V[size_t(i) * n + r]);
+        y[r] = T(s);
+    }
+}
+template <class A, class B>
+__global__ void convert(int n, const A* __restrict__ x, B* __restrict__ y, double scale) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) y[r] = B(double(x[r]) * scale);
+}
+// x += alpha * d
+template <class T>
+__global__ void axpy_into(int n, double alpha, const T* __restrict__ d, double* __restrict__ x) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) x[r] += alpha * double(d[r]);
+}
+
+template <class T>
+__global__ void sub_from(int n, const T* __restrict__ b, const T* __restrict__ a, T* __restrict__ out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) out[r] = b[r] - a[r];
+}
+template <class T>
+__global__ void scale_by(int n, const T* __restrict__ x, double a, T* __restrict__ y) {
+    const T aa = T(a);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) y[r] = x[r] * aa;
+}
+template <class T>
+__global__ void add_to(int n, const T* __restrict__ d, T* __restrict__ x) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) x[r] += d[r];
+}
+
+int vgrid(int n) {
+    long b = (long(n) + 255) / 256;
+    return int(b < 152 * 4 ? b : 152 * 4);
+}
 int spmv_grid(int nrows) {
     long blocks = (long(nrows) * 4 + 255) / 256;
     return int(blocks < 152 * 8 ? blocks : 152 * 8);
@@ -38,6 +163,24 @@ void launch_spmv32(int nrows, const int* rp, const int* ci, const float* v, cons
     spmv_csr4<float><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y);
 }
 
+// Krylov workspace (both precisions share the layout)
+struct Krylov {
+    int n = 0, m = 0, nblk = 0;
+    void* V = nullptr;       // (m+1) x n in the Krylov precision
+    void* w = nullptr;       // n
+    void* z = nullptr;       // n
+    double* part = nullptr;  // nblk x (m+1)
+    double* dots = nullptr;  // m+1
+    double* h = nullptr;     // m+1 (current Hessenberg column)
+    double* y = nullptr;     // m
+    double* r64 = nullptr;   // n
+    double* x64 = nullptr;   // n
+    double* hpin = nullptr;  // pinned host copy of h
+    void* rhsT = nullptr;    // n, Krylov precision: normalised rhs of an inner solve
+    void* xT = nullptr;      // n, Krylov precision: inner solution
+    int prec = -1;
+};
+
 void Engine::spmv64(const double* x, double* y) {
     launch_spmv64(ndim, d_rowptr, d_col, d_val, x, y, stream);
     ck(cudaGetLastError());
@@ -47,10 +190,286 @@ void Engine::spmv32(const float* x, float* y) {
     ck(cudaGetLastError());
 }
 
-void Engine::free_solver() {}
-void Engine::ensure_solver() {}
-void Engine::build_preconditioner(int) { throw EngineError(IEMIC_ERR_STATE); }
-int Engine::solve_dev(const double*, double*, const iemic_solve_opts&, iemic_solve_stats&) { return IEMIC_ERR_STATE; }
-void Engine::apply_precon(int, const double*, double*) { throw EngineError(IEMIC_ERR_STATE); }
+void Engine::free_solver() {
+    delete lu64;
+    delete lu32;
+    lu64 = lu32 = nullptr;
+    if (kry) {
+        cudaFree(kry->V); cudaFree(kry->w); cudaFree(kry->z); cudaFree(kry->part); cudaFree(kry->dots);
+        cudaFree(kry->h); cudaFree(kry->y); cudaFree(kry->r64); cudaFree(kry->x64);
+        cudaFree(kry->rhsT); cudaFree(kry->xT);
+        cudaFreeHost(kry->hpin);
+        delete kry;
+        kry = nullptr;
+    }
+    delete ndplan;
+    ndplan = nullptr;
+}
+
+void Engine::ensure_solver() {
+    if (!ndplan) {
+        ndplan = new NdPlan();
+        build_nd_plan(*ndplan, cfg.n, cfg.m, cfg.l, cfg.periodic ? 1 : 0, landm, row_ptr, host_col_idx(), 32);
+    }
+}
+
+const std::vector<int>& Engine::host_col_idx() {
+    if (h_col.empty()) {
+        h_col.resize(size_t(nnz));
+        ck(cudaMemcpyAsync(h_col.data(), d_col, sizeof(int) * size_t(nnz), cudaMemcpyDeviceToHost, stream));
+        ck(cudaStreamSynchronize(stream));
+    }
+    return h_col;
+}
+
+static void ensure_krylov(Engine& e, int m, int prec) {
+    Krylov*& k = e.kry;
+    const size_t ts = prec ? sizeof(float) : sizeof(double);
+    if (k && k->m >= m && k->prec == prec) return;
+    if (k) {
+        cudaFree(k->V); cudaFree(k->w); cudaFree(k->z); cudaFree(k->part); cudaFree(k->dots);
+        cudaFree(k->h); cudaFree(k->y); cudaFree(k->r64); cudaFree(k->x64);
+        cudaFree(k->rhsT); cudaFree(k->xT);
+        cudaFreeHost(k->hpin);
+        delete k;
+    }
+    k = new Krylov();
+    k->n = e.ndim;
+    k->m = m;
+    k->prec = prec;
+    k->nblk = vgrid(e.ndim);
+    auto A = [&](size_t bytes) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) throw EngineError(IEMIC_ERR_NOMEM);
+        return p;
+    };
+    k->V = A(ts * size_t(m + 1) * e.ndim);
+    k->w = A(ts * e.ndim);
+    k->z = A(ts * e.ndim);
+    k->part = static_cast<double*>(A(sizeof(double) * size_t(k->nblk) * (m + 1)));
+    k->dots = static_cast<double*>(A(sizeof(double) * (m + 2)));
+    k->h = static_cast<double*>(A(sizeof(double) * (m + 2)));
+    k->y = static_cast<double*>(A(sizeof(double) * (m + 2)));
+    k->r64 = static_cast<double*>(A(sizeof(double) * e.ndim));
+    k->x64 = static_cast<double*>(A(sizeof(double) * e.ndim));
+    k->rhsT = A(ts * e.ndim);
+    k->xT = A(ts * e.ndim);
+    ck(cudaMallocHost(&k->hpin, sizeof(double) * (m + 2)));
+}
+
+NdLu*& Engine::lu_for(int precision) { return precision == IEMIC_PREC_MIXED ? lu32 : lu64; }
+
+void Engine::build_preconditioner(int precision) {
+    if (!jac_valid) throw EngineError(IEMIC_ERR_STATE);
+    ensure_solver();
+    NdLu*& lu = lu_for(precision);
+    if (!lu) {
+        lu = new NdLu();
+        ndlu_setup(*lu, *ndplan, precision == IEMIC_PREC_MIXED ? 1 : 0);
+    }
+    ndlu_factor(*lu, d_rowptr, d_col, d_val, stream);
+    ck(cudaStreamSynchronize(stream));
+    if (precision == IEMIC_PREC_MIXED) fact32_stale = false; else fact64_stale = false;
+}
+
+void Engine::apply_precon(int precision, const double* v, double* out) {
+    NdLu* lu = lu_for(precision);
+    if (!lu || !lu->factored) throw EngineError(IEMIC_ERR_STATE);
+    if (precision == IEMIC_PREC_MIXED) {
+        ensure_krylov(*this, kry ? kry->m : 100, 1);
+        float* w = static_cast<float*>(kry->w);
+        float* z = static_cast<float*>(kry->z);
+        convert<double, float><<<vgrid(ndim), 256, 0, stream>>>(ndim, v, w, 1.0);
+        ndlu_apply(*lu, d_rowptr, d_col, d_val, w, z, 1, stream);
+        convert<float, double><<<vgrid(ndim), 256, 0, stream>>>(ndim, z, out, 1.0);
+    } else {
+        ndlu_apply(*lu, d_rowptr, d_col, d_val, v, out, 0, stream);
+    }
+    ck(cudaGetLastError());
+}
+
+// One restarted-GMRES solve of J x = b in precision T, x0 = 0, right
+// preconditioned by the factorisation `lu`. `b` must not alias the Krylov
+// workspace. Returns the inner iterations used.
+template <class T>
+static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, int maxit, double tol,
+                 double* relres_out) {
+    Krylov& K = *e.kry;
+    const int n = e.ndim;
+    cudaStream_t s = e.stream;
+    T* V = static_cast<T*>(K.V);
+    T* w = static_cast<T*>(K.w);
+    T* z = static_cast<T*>(K.z);
+    const int G = vgrid(n);
+    auto dot = [&](const T* a, const T* c) {
+        multidot<T><<<G, 256, 0, s>>>(n, 1, a == c ? a : a, c, K.part);
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+        ck(cudaMemcpyAsync(K.hpin, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+        ck(cudaStreamSynchronize(s));
+        return K.hpin[0];
+    };
+    std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    ck(cudaMemsetAsync(x, 0, sizeof(T) * n, s));
+    const double beta0 = std::sqrt(dot(b, b));
+    if (!(beta0 > 0.0)) {
+        *relres_out = 0.0;
+        return 0;
+    }
+    if (!std::isfinite(beta0)) throw EngineError(IEMIC_ERR_NAN);
+    int it = 0;
+    double relres = 1.0;
+    bool first = true;
+    while (true) {
+        // r = b - J x  (x = 0 on the first cycle)
+        if (first) {
+            ck(cudaMemcpyAsync(w, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+        } else {
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, x, z);
+            sub_from<T><<<G, 256, 0, s>>>(n, b, z, w);
+        }
+        first = false;
+        const double beta = std::sqrt(dot(w, w));
+        if (!std::isfinite(beta)) throw EngineError(IEMIC_ERR_NAN);
+        relres = beta / beta0;
+        if (relres <= tol || it >= maxit) break;
+        scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / beta, V);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && it < maxit;) {
+            ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, V + size_t(j) * n, z, sizeof(T) == 4, s);
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, z, w);
+            for (int pass = 0; pass < 2; ++pass) {   // CGS2
+                multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part);
+                reduce_parts<<<1, 256, 0, s>>>(G, j + 1, K.part, K.dots, K.h, pass == 0);
+                basis_update<T><<<G, 256, 0, s>>>(n, j + 1, V, K.dots, w);
+            }
+            multidot<T><<<G, 256, 0, s>>>(n, 1, w, w, K.part);
+            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0);
+            ck(cudaMemcpyAsync(K.hpin, K.h, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, s));
+            ck(cudaStreamSynchronize(s));
+            const double hn = std::sqrt(K.hpin[j + 1]);
+            if (!std::isfinite(hn)) throw EngineError(IEMIC_ERR_NAN);
+            if (hn > 0.0) scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / hn, V + size_t(j + 1) * n);
+            for (int i = 0; i <= j; ++i) H[size_t(i) * m + j] = K.hpin[i];
+            H[size_t(j + 1) * m + j] = hn;
+            for (int i = 0; i < j; ++i) {   // apply the previous Givens rotations
+                double a = H[size_t(i) * m + j], c = H[size_t(i + 1) * m + j];
+                H[size_t(i) * m + j] = cs[i] * a + sn[i] * c;
+                H[size_t(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+            }
+            double a = H[size_t(j) * m + j], c = H[size_t(j + 1) * m + j];
+            double d = std::hypot(a, c);
+            cs[j] = d > 0 ? a / d : 1.0;
+            sn[j] = d > 0 ? c / d : 0.0;
+            H[size_t(j) * m + j] = d;
+            H[size_t(j + 1) * m + j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++j;
+            ++it;
+            relres = std::fabs(g[j]) / beta0;
+            if (relres <= tol || hn == 0.0) break;
+        }
+        // y = H^{-1} g (FP64 back substitution), x += M^{-1} (V y)
+        for (int i = j - 1; i >= 0; --i) {
+            double sum = g[i];
+            for (int q = i + 1; q < j; ++q) sum -= H[size_t(i) * m + q] * y[q];
+            y[i] = sum / H[size_t(i) * m + i];
+        }
+        ck(cudaMemcpyAsync(K.y, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        combine<T><<<G, 256, 0, s>>>(n, j, V, K.y, w);
+        ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, w, z, sizeof(T) == 4, s);
+        add_to<T><<<G, 256, 0, s>>>(n, z, x);
+        ck(cudaStreamSynchronize(s));   // y is a host temporary
+    }
+    ck(cudaGetLastError());
+    *relres_out = relres;
+    return it;
+}
+
+int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
+    if (!jac_valid) return IEMIC_ERR_STATE;
+    if (o.transpose) return solve_transpose_dev(b, x, o, st);
+    const int prec = o.precision == IEMIC_PREC_MIXED ? IEMIC_PREC_MIXED : IEMIC_PREC_FP64;
+    auto t0 = std::chrono::steady_clock::now();
+    ensure_solver();
+    NdLu*& lu = lu_for(prec);
+    bool stale = prec == IEMIC_PREC_MIXED ? fact32_stale : fact64_stale;
+    if (!lu || !lu->factored || (stale && !o.reuse_preconditioner)) {
+        build_preconditioner(prec);
+        st.factorizations += 1;
+    }
+    st.perturbed_pivots = lu->npert;
+    auto t1 = std::chrono::steady_clock::now();
+    st.time_factor_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    ensure_krylov(*this, o.restart, prec);
+    Krylov& K = *kry;
+    const int n = ndim;
+    const int G = vgrid(n);
+    cudaStream_t s = stream;
+    // ||b||
+    multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part);
+    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+    double bn2 = 0.0;
+    ck(cudaMemcpyAsync(&bn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    const double bnorm = std::sqrt(bn2);
+    if (!std::isfinite(bnorm)) return IEMIC_ERR_NAN;
+    ck(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    if (bnorm == 0.0) {
+        st.relres = 0.0;
+        return IEMIC_OK;
+    }
+    int rc = IEMIC_OK;
+    double relres = 1.0;
+    if (prec == IEMIC_PREC_FP64) {
+        scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64);
+        double est = 1.0;
+        st.iters += gmres<double>(*this, *lu, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est);
+        axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x);
+        residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64);
+        multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part);
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+        double rn2 = 0.0;
+        ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+        ck(cudaStreamSynchronize(s));
+        relres = std::sqrt(rn2) / bnorm;
+    } else {
+        // FP64 iterative refinement around FP32 GMRES
+        float* r32 = static_cast<float*>(K.rhsT);
+        float* d32 = static_cast<float*>(K.xT);
+        ck(cudaMemcpyAsync(K.r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        double rnorm = bnorm;
+        for (int ref = 0;; ++ref) {
+            relres = rnorm / bnorm;
+            if (!std::isfinite(relres)) return IEMIC_ERR_NAN;
+            if (relres <= o.tol) break;
+            if (ref >= o.max_refinements || st.iters >= o.max_iters) break;
+            convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm);
+            double est = 1.0;
+            double inner = std::max(o.inner_tol, 0.5 * o.tol / relres);
+            st.iters += gmres<float>(*this, *lu, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner, &est);
+            axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x);
+            residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64);
+            multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part);
+            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+            double rn2 = 0.0;
+            ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+            ck(cudaStreamSynchronize(s));
+            rnorm = std::sqrt(rn2);
+            st.refinements += 1;
+        }
+    }
+    st.relres = relres;
+    auto t2 = std::chrono::steady_clock::now();
+    st.time_solve_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
+    if (relres > o.tol) rc = IEMIC_ERR_NOT_CONVERGED;
+    return rc;
+}
+
+int Engine::solve_transpose_dev(const double*, double*, const iemic_solve_opts&, iemic_solve_stats&) {
+    return IEMIC_ERR_STATE;
+}
 
 }  // namespace iemic

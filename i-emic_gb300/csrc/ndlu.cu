@@ -1,0 +1,937 @@
+// Nested-dissection multilevel block LU of the THCM Jacobian.
+//
+// The reference preconditions its FGMRES with an ILU/MRILU-based block
+// scheme (src/trios/TRIOS_BlockPreconditioner.C, src/mrilucpp). On the full
+// saddle-point Jacobian, zero-fill ILU variants do not converge (W and P rows
+// have zero diagonals, and the B-grid pressure has constant and checkerboard
+// null modes). This preconditioner therefore follows MRILU's multilevel idea
+// with drop tolerance 0: eliminate an independent set, form the Schur
+// complement, recurse. The independent sets come from a nested dissection of
+// the grid's water columns. Each elimination tree node is a dense frontal
+// matrix: batched panel LU with block-local partial pivoting, tiled GEMM
+// Schur updates and extend-add into the parent.
+//
+// Three kinds of unknowns are left out of the factorisation: unknowns whose
+// Jacobian rows are identities (land cells, velocity points next to land,
+// surface w; src/ocean/boundary.F90), and two pinned pressures per surface
+// basin, the rows src/ocean/THCM.C:2260-2297 (fixPressurePoints) would
+// replace. So the factor preconditions the original, singular-but-consistent
+// J.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <numeric>
+#include <unordered_map>
+
+#include "engine.cuh"
+#include "ndlu.cuh"
+#include "stencil.cuh"
+
+namespace iemic {
+
+// ===========================================================================
+// symbolic analysis (host, once per land mask)
+// ===========================================================================
+namespace {
+
+struct Node {
+    std::vector<int> cols;        // own water columns (i + n*j)
+    int i0, i1, j0, j1;           // region of the subtree
+    int child[2] = {-1, -1};
+    int nchild = 0;
+    int parent = -1;
+    int height = 0;
+};
+
+}  // namespace
+
+void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::vector<int>& landm,
+                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel) {
+    plan = NdPlan();
+    plan.panel = panel;
+    const int ndim = NUN * n * m * l;
+    plan.ndim = ndim;
+    auto LM = [&](int i, int j, int k) { return landm[i + (n + 2) * (j + (m + 2) * k)]; };
+    auto grow = [&](int i, int j, int k, int t) { return NUN * (i + n * (j + m * k)) + t; };   // 0-based
+
+    // 1. dry unknowns: identity rows made by boundaries() (src/ocean/boundary.F90)
+    std::vector<char> dry(ndim, 0);
+    for (int k = 1; k <= l; ++k)
+        for (int j = 1; j <= m; ++j)
+            for (int i = 1; i <= n; ++i) {
+                int base = grow(i - 1, j - 1, k - 1, 0);
+                if (LM(i, j, k) != OCEAN) {
+                    for (int t = 0; t < NUN; ++t) dry[base + t] = 1;
+                    continue;
+                }
+                if (LM(i, j + 1, k) == LAND || LM(i + 1, j, k) == LAND || LM(i + 1, j + 1, k) == LAND) {
+                    dry[base + 0] = 1;
+                    dry[base + 1] = 1;
+                }
+                if (LM(i, j, k + 1) == LAND) dry[base + 2] = 1;
+            }
+    // 2. barotropic pressure of every water column. A column's pressures are
+    //    tied together by its hydrostatic w rows, so one pressure per column (at
+    //    the surface) carries its depth-independent mode; that mode couples
+    //    only through horizontal velocity points. Columns are connected when
+    //    an active velocity point (any level) touches both. Per connected
+    //    component, two adjacent surface pressures (one for a single column)
+    //    are pinned, as THCM's fixPressurePoints rows would pin them
+    //    (src/ocean/THCM.C:2260-2297): this removes the constant and
+    //    checkerboard null modes of J from the preconditioner.
+    std::vector<char> ocean_col(size_t(n) * m, 0), uv_col(size_t(n) * m, 0);
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) {
+            ocean_col[i + n * j] = LM(i + 1, j + 1, l) == OCEAN;
+            for (int k = 0; k < l; ++k)
+                if (!dry[grow(i, j, k, 0)] || !dry[grow(i, j, k, 1)]) uv_col[i + n * j] = 1;
+        }
+    {
+        std::vector<int> uf(size_t(n) * m);
+        std::iota(uf.begin(), uf.end(), 0);
+        std::function<int(int)> find = [&](int a) {
+            while (uf[a] != a) { uf[a] = uf[uf[a]]; a = uf[a]; }
+            return a;
+        };
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < n; ++i) {
+                if (!uv_col[i + n * j]) continue;
+                const int di[3] = {1, 0, 1}, dj[3] = {0, 1, 1};
+                for (int d = 0; d < 3; ++d) {
+                    int ii = i + di[d], jj = j + dj[d];
+                    if (periodic) ii %= n;
+                    if (ii >= n || jj >= m || !ocean_col[ii + n * jj]) continue;
+                    uf[find(i + n * j)] = find(ii + n * jj);
+                }
+            }
+        std::vector<std::vector<int>> comps(size_t(n) * m);
+        for (int j = m - 1; j >= 0; --j)      // scan from the north-east corner
+            for (int i = n - 1; i >= 0; --i)
+                if (ocean_col[i + n * j]) comps[find(i + n * j)].push_back(i + n * j);
+        for (auto& K : comps) {
+            if (K.empty()) continue;
+            std::vector<char> in(size_t(n) * m, 0);
+            for (int c : K) in[c] = 1;
+            bool done = false;
+            for (int c : K) {   // a horizontally adjacent pair first
+                int i = c % n, j = c / n, iw = periodic ? (i - 1 + n) % n : i - 1;
+                if (iw >= 0 && in[iw + n * j]) {
+                    plan.pins.push_back(grow(i, j, l - 1, PP - 1));
+                    plan.pins.push_back(grow(iw, j, l - 1, PP - 1));
+                    done = true;
+                    break;
+                }
+            }
+            for (size_t q = 0; q < K.size() && !done; ++q) {
+                int i = K[q] % n, j = K[q] / n;
+                if (j > 0 && in[i + n * (j - 1)]) {
+                    plan.pins.push_back(grow(i, j, l - 1, PP - 1));
+                    plan.pins.push_back(grow(i, j - 1, l - 1, PP - 1));
+                    done = true;
+                }
+            }
+            if (!done) plan.pins.push_back(grow(K[0] % n, K[0] / n, l - 1, PP - 1));
+        }
+        for (int p : plan.pins) dry[p] = 1;
+    }
+    for (int r = 0; r < ndim; ++r)
+        if (dry[r]) plan.dry_rows.push_back(r);
+    // deferred unknowns: the surface pressure of every (unpinned) water column
+    // is eliminated in the root front, so no subdomain block contains a
+    // floating barotropic pressure mode.
+    std::vector<char> deferred(ndim, 0);
+    std::vector<int> deferred_list;
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) {
+            int g = grow(i, j, l - 1, PP - 1);
+            if (ocean_col[i + n * j] && !dry[g]) {
+                deferred[g] = 1;
+                deferred_list.push_back(g);
+            }
+        }
+
+    // 3. wet unknowns per water column, ordered (k, t)
+    std::vector<std::vector<int>> colvars(size_t(n) * m);
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < l; ++k)
+                for (int t = 0; t < NUN; ++t) {
+                    int g = grow(i, j, k, t);
+                    if (!dry[g] && !deferred[g]) colvars[i + n * j].push_back(g);
+                }
+
+    // 4. nested dissection of the column grid (postorder)
+    std::vector<Node> nodes;
+    const int LEAF = 4;
+    std::function<int(int, int, int, int)> rec = [&](int i0, int i1, int j0, int j1) -> int {
+        int W = i1 - i0, H = j1 - j0;
+        if (W <= 0 || H <= 0) return -1;
+        Node nd;
+        nd.i0 = i0; nd.i1 = i1; nd.j0 = j0; nd.j1 = j1;
+        int c0 = -1, c1 = -1;
+        if (W * H <= LEAF) {
+            for (int j = j0; j < j1; ++j)
+                for (int i = i0; i < i1; ++i) nd.cols.push_back(((i % n) + n) % n + n * j);
+        } else if (W >= H) {
+            int im = i0 + W / 2;
+            c0 = rec(i0, im, j0, j1);
+            c1 = rec(im + 1, i1, j0, j1);
+            for (int j = j0; j < j1; ++j) nd.cols.push_back(((im % n) + n) % n + n * j);
+        } else {
+            int jm = j0 + H / 2;
+            c0 = rec(i0, i1, j0, jm);
+            c1 = rec(i0, i1, jm + 1, j1);
+            for (int i = i0; i < i1; ++i) nd.cols.push_back(((i % n) + n) % n + n * jm);
+        }
+        for (int c : {c0, c1})
+            if (c >= 0) nd.child[nd.nchild++] = c;
+        nodes.push_back(nd);
+        int id = int(nodes.size()) - 1;
+        for (int q = 0; q < nodes[id].nchild; ++q) nodes[nodes[id].child[q]].parent = id;
+        return id;
+    };
+    int root = -1;
+    if (periodic) {
+        int h = n / 2;
+        int c0 = rec(1, h, 0, m);
+        int c1 = rec(h + 1, n, 0, m);
+        Node nd;
+        nd.i0 = 0; nd.i1 = n; nd.j0 = 0; nd.j1 = m;
+        for (int j = 0; j < m; ++j) nd.cols.push_back(0 + n * j);
+        for (int j = 0; j < m; ++j) nd.cols.push_back(h + n * j);
+        for (int c : {c0, c1})
+            if (c >= 0) nd.child[nd.nchild++] = c;
+        nodes.push_back(nd);
+        root = int(nodes.size()) - 1;
+        for (int q = 0; q < nodes[root].nchild; ++q) nodes[nodes[root].child[q]].parent = root;
+    } else {
+        root = rec(0, n, 0, m);
+    }
+    const int NF = int(nodes.size());
+    for (int f = 0; f < NF; ++f) {   // postorder: children precede parents
+        int h = 0;
+        for (int q = 0; q < nodes[f].nchild; ++q) h = std::max(h, nodes[nodes[f].child[q]].height + 1);
+        nodes[f].height = h;
+    }
+
+    // 5. reduced ordering: own unknowns of the fronts in postorder
+    plan.g2r.assign(ndim, -1);
+    plan.fronts.resize(NF);
+    std::vector<int> owner;
+    for (int f = 0; f < NF; ++f) {
+        FrontDev& fr = plan.fronts[f];
+        fr.red0 = int(plan.r2g.size());
+        std::vector<int> own;
+        for (int c : nodes[f].cols)
+            for (int g : colvars[c]) own.push_back(g);
+        if (f == root) own.insert(own.end(), deferred_list.begin(), deferred_list.end());
+        for (int g : own) {
+            plan.g2r[g] = int(plan.r2g.size());
+            plan.r2g.push_back(g);
+            owner.push_back(f);
+        }
+        fr.nf = int(plan.r2g.size()) - fr.red0;
+        fr.parent = nodes[f].parent;
+    }
+    plan.nred = int(plan.r2g.size());
+
+    // 6. boundary unknowns: the non-deferred unknowns of the ring of columns
+    //    around the subtree region, plus the deferred surface pressures of the
+    //    region and the ring (all owned by ancestors), sorted by reduced index
+    std::vector<std::vector<int>> bvars(NF);
+    for (int f = 0; f < NF; ++f) {
+        if (nodes[f].parent < 0) continue;
+        const Node& nd = nodes[f];
+        std::vector<int> ring, region;
+        for (int j = nd.j0 - 1; j <= nd.j1; ++j)
+            for (int i = nd.i0 - 1; i <= nd.i1; ++i) {
+                if (j < 0 || j >= m) continue;
+                int ii = i;
+                if (periodic) ii = (i % n + n) % n;
+                else if (i < 0 || i >= n) continue;
+                bool inside = i >= nd.i0 && i < nd.i1 && j >= nd.j0 && j < nd.j1;
+                (inside ? region : ring).push_back(ii + n * j);
+            }
+        std::sort(ring.begin(), ring.end());
+        ring.erase(std::unique(ring.begin(), ring.end()), ring.end());
+        for (int c : ring)
+            for (int g : colvars[c]) bvars[f].push_back(plan.g2r[g]);
+        for (auto* cols : {&region, &ring})
+            for (int c : *cols) {
+                int g = grow(c % n, c / n, l - 1, PP - 1);
+                if (deferred[g]) bvars[f].push_back(plan.g2r[g]);
+            }
+        std::sort(bvars[f].begin(), bvars[f].end());
+        bvars[f].erase(std::unique(bvars[f].begin(), bvars[f].end()), bvars[f].end());
+    }
+    auto local = [&](int f, int red) -> int {
+        const FrontDev& fr = plan.fronts[f];
+        if (red >= fr.red0 && red < fr.red0 + fr.nf) return red - fr.red0;
+        auto it = std::lower_bound(bvars[f].begin(), bvars[f].end(), red);
+        if (it == bvars[f].end() || *it != red) return -1;
+        return fr.nf + int(it - bvars[f].begin());
+    };
+
+    // 7. offsets, var lists, extend-add maps
+    int64_t off = 0, dinv = 0, voff = 0, eoff = 0, woff = 0;
+    plan.child_slot.assign(NF, -1);
+    for (int f = 0; f < NF; ++f) {
+        FrontDev& fr = plan.fronts[f];
+        fr.nb = int(bvars[f].size());
+        fr.F = fr.nf + fr.nb;
+        fr.off = off;
+        off += int64_t(fr.F) * fr.F;
+        fr.dinv_off = dinv;
+        dinv += int64_t((fr.nf + panel - 1) / panel) * 2 * panel * panel;
+        fr.voff = voff;
+        voff += fr.F;
+        for (int q = 0; q < fr.nf; ++q) plan.vars.push_back(fr.red0 + q);
+        for (int r : bvars[f]) plan.vars.push_back(r);
+        fr.woff = woff;
+        woff += fr.F;
+        fr.emap_off = eoff;
+        for (int q = 0; q < nodes[f].nchild; ++q) plan.child_slot[nodes[f].child[q]] = q;
+        const double a = fr.nf, b = fr.nb;
+        plan.flops += 2.0 / 3.0 * a * a * a + 2.0 * a * a * b + 2.0 * a * b * b;
+        plan.factor_entries += int64_t(fr.nf) * fr.nf + 2 * int64_t(fr.nf) * fr.nb;
+    }
+    for (int f = 0; f < NF; ++f) {
+        FrontDev& fr = plan.fronts[f];
+        fr.emap_off = eoff;
+        if (fr.parent >= 0)
+            for (int r : bvars[f]) {
+                int loc = local(fr.parent, r);
+                if (loc < 0) throw EngineError(IEMIC_ERR_STATE);   // broken tree invariant
+                plan.emap.push_back(loc);
+                ++eoff;
+            }
+    }
+    plan.front_entries = off;
+    plan.dinv_entries = dinv;
+    plan.emap_entries = eoff;
+    plan.w_entries = woff;
+    plan.nfronts = NF;
+
+    // 8. levels by height; children lists per parent level and slot
+    int H = 0;
+    for (int f = 0; f < NF; ++f) H = std::max(H, nodes[f].height + 1);
+    plan.nlevels = H;
+    plan.level_fronts.assign(H, {});
+    plan.level_children[0].assign(H, {});
+    plan.level_children[1].assign(H, {});
+    for (int f = 0; f < NF; ++f) plan.level_fronts[nodes[f].height].push_back(f);
+    for (int f = 0; f < NF; ++f)
+        if (nodes[f].parent >= 0)
+            plan.level_children[plan.child_slot[f]][nodes[nodes[f].parent].height].push_back(f);
+    plan.level_maxnf.assign(H, 0);
+    plan.level_maxF.assign(H, 0);
+    for (int h = 0; h < H; ++h)
+        for (int f : plan.level_fronts[h]) {
+            plan.level_maxnf[h] = std::max(plan.level_maxnf[h], plan.fronts[f].nf);
+            plan.level_maxF[h] = std::max(plan.level_maxF[h], plan.fronts[f].F);
+        }
+
+    // 9. assembly map: entry (r, c) goes to the front that eliminates the
+    //    earlier of its two unknowns
+    for (int r = 0; r < ndim; ++r) {
+        int rr = plan.g2r[r];
+        if (rr < 0) continue;
+        for (int q = row_ptr[r]; q < row_ptr[r + 1]; ++q) {
+            int rc = plan.g2r[col_idx[q]];
+            if (rc < 0) continue;
+            int f = owner[std::min(rr, rc)];
+            int lr = local(f, rr), lc = local(f, rc);
+            if (lr < 0 || lc < 0) throw EngineError(IEMIC_ERR_STATE);
+            const FrontDev& fr = plan.fronts[f];
+            plan.asm_src.push_back(q);
+            plan.asm_row.push_back(r);
+            plan.asm_dst.push_back(fr.off + int64_t(lc) * fr.F + lr);
+        }
+    }
+}
+
+// ===========================================================================
+// numeric kernels
+// ===========================================================================
+namespace {
+
+constexpr int NT = 256;    // threads of the per-front solve kernels
+constexpr int NTP = 512;   // threads of the panel kernel
+
+__device__ __forceinline__ double atomic_max_pos(double* a, double v) {
+    // non-negative doubles order like their bit patterns
+    unsigned long long* p = reinterpret_cast<unsigned long long*>(a);
+    return __longlong_as_double(atomicMax(p, __double_as_longlong(v)));
+}
+
+// Ruiz equilibration of the wet block: one pass of row then column scaling
+// by the square root of the largest scaled magnitude.
+__global__ void k_rowmax(int ndim, const int* __restrict__ g2r, const int* __restrict__ rp, const int* __restrict__ ci,
+                         const double* __restrict__ v, const double* __restrict__ dc, double* __restrict__ dr) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ndim; r += gridDim.x * blockDim.x) {
+        if (g2r[r] < 0) continue;
+        double mx = 0.0;
+        for (int q = rp[r]; q < rp[r + 1]; ++q)
+            if (g2r[ci[q]] >= 0) mx = fmax(mx, fabs(v[q]) * dc[ci[q]]);
+        mx *= dr[r];
+        if (mx > 0.0) dr[r] /= sqrt(mx);
+    }
+}
+__global__ void k_colmax(int ndim, const int* __restrict__ g2r, const int* __restrict__ rp, const int* __restrict__ ci,
+                         const double* __restrict__ v, const double* __restrict__ dr, const double* __restrict__ dc,
+                         double* __restrict__ cmax) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ndim; r += gridDim.x * blockDim.x) {
+        if (g2r[r] < 0) continue;
+        for (int q = rp[r]; q < rp[r + 1]; ++q) {
+            int c = ci[q];
+            if (g2r[c] >= 0) atomic_max_pos(cmax + c, fabs(dr[r] * v[q] * dc[c]));
+        }
+    }
+}
+__global__ void k_colscale(int ndim, const int* __restrict__ g2r, const double* __restrict__ cmax,
+                           double* __restrict__ dc) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ndim; c += gridDim.x * blockDim.x)
+        if (g2r[c] >= 0 && cmax[c] > 0.0) dc[c] /= sqrt(cmax[c]);
+}
+
+template <class T>
+__global__ void k_assemble(int64_t n, const int* __restrict__ src, const int64_t* __restrict__ dst,
+                           const int* __restrict__ rowof, const int* __restrict__ ci, const double* __restrict__ val,
+                           const double* __restrict__ dr, const double* __restrict__ dc, T* __restrict__ front) {
+    for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < n; q += int64_t(gridDim.x) * blockDim.x) {
+        const int e = src[q];
+        front[dst[q]] = T(dr[rowof[q]] * val[e] * dc[ci[e]]);
+    }
+}
+
+// front[parent] += S[child] for the children in `list` (one slot at a time)
+template <class T>
+__global__ void k_extend_add(const FrontDev* __restrict__ fronts, const int* __restrict__ list,
+                             const int* __restrict__ emap, T* __restrict__ front) {
+    const FrontDev c = fronts[list[blockIdx.y]];
+    const FrontDev p = fronts[c.parent];
+    const int64_t tot = int64_t(c.nb) * c.nb;
+    const int* em = emap + c.emap_off;
+    const T* S = front + c.off;
+    T* P = front + p.off;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+        int a = int(e % c.nb), b = int(e / c.nb);   // row a, column b of S
+        P[int64_t(em[b]) * p.F + em[a]] += S[int64_t(c.nf + b) * c.F + c.nf + a];
+    }
+}
+
+// Panel p of every front of a level: LU with partial pivoting over all the
+// front's fully-summed rows [j, nf) for columns p..p+bb-1, applied to the
+// whole panel height (this also yields L21 for the boundary rows). Then the
+// inverses of the diagonal block's unit-lower and upper factors are stored for
+// the U12 update and the solve phase.
+template <class T, int B>
+__global__ void __launch_bounds__(NTP) k_panel(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
+                                               T* __restrict__ front, T* __restrict__ dinv, int* __restrict__ piv,
+                                               T tau, int* __restrict__ npert) {
+    const FrontDev fr = fronts[lf[blockIdx.x]];
+    if (fr.nf <= p) return;
+    const int bb = min(B, fr.nf - p), F = fr.F, nf = fr.nf, tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    T* A = front + fr.off;
+    __shared__ T wv[NTP / 32];
+    __shared__ int wr[NTP / 32];
+    __shared__ int prow;
+    __shared__ T S[B][B + 1];
+    __shared__ T X[B][B + 1];
+    for (int jj = 0; jj < bb; ++jj) {
+        const int j = p + jj;
+        T* colj = A + int64_t(j) * F;
+        // pivot search over rows [j, nf)
+        T bv = T(-1);
+        int br = j;
+        for (int r = j + tid; r < nf; r += NTP) {
+            T v = abs(colj[r]);
+            if (v > bv) { bv = v; br = r; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            int orr = __shfl_xor_sync(0xffffffffu, br, o);
+            if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
+        }
+        if (lane == 0) { wv[warp] = bv; wr[warp] = br; }
+        __syncthreads();
+        if (tid == 0) {
+            T b0 = wv[0];
+            int r0 = wr[0];
+            for (int q = 1; q < NTP / 32; ++q)
+                if (wv[q] > b0 || (wv[q] == b0 && wr[q] < r0)) { b0 = wv[q]; r0 = wr[q]; }
+            prow = r0;
+            piv[fr.red0 + j] = r0;
+        }
+        __syncthreads();
+        const int pr = prow;
+        if (pr != j)   // swap whole panel rows
+            for (int c = tid; c < bb; c += NTP) {
+                T* col = A + int64_t(p + c) * F;
+                T t = col[j];
+                col[j] = col[pr];
+                col[pr] = t;
+            }
+        __syncthreads();
+        if (tid == 0) {
+            T d = colj[j];
+            T scale = T(0);
+            for (int c = 0; c < bb; ++c) scale = max(scale, abs(A[int64_t(p + c) * F + j]));
+            if (!(abs(d) > tau * scale)) {
+                colj[j] = (d < T(0) ? -tau : tau) * (scale > T(0) ? scale : T(1));
+                atomicAdd(npert, 1);
+            }
+        }
+        __syncthreads();
+        const T dinvv = T(1) / colj[j];
+        for (int r = j + 1 + tid; r < F; r += NTP) colj[r] *= dinvv;
+        __syncthreads();
+        // rank-1 update of the remaining panel columns
+        const int wcols = bb - jj - 1;
+        if (wcols > 0) {
+            const int64_t tot = int64_t(F - j - 1) * wcols;
+            for (int64_t e = tid; e < tot; e += NTP) {
+                int r = j + 1 + int(e % (F - j - 1));
+                int c = p + jj + 1 + int(e / (F - j - 1));
+                A[int64_t(c) * F + r] -= colj[r] * A[int64_t(c) * F + j];
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < bb * bb; e += NTP) S[e % bb][e / bb] = A[int64_t(p + e / bb) * F + p + e % bb];
+    __syncthreads();
+    if (tid < bb) {   // inverse of the unit-lower factor
+        const int c = tid;
+        for (int r = 0; r < bb; ++r) X[r][c] = T(0);
+        X[c][c] = T(1);
+        for (int r = c + 1; r < bb; ++r) {
+            T s = T(0);
+            for (int q = c; q < r; ++q) s += S[r][q] * X[q][c];
+            X[r][c] = -s;
+        }
+    }
+    __syncthreads();
+    T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
+    for (int e = tid; e < B * B; e += NTP) Di[e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
+    __syncthreads();
+    if (tid < bb) {   // inverse of the upper factor
+        const int c = tid;
+        for (int r = 0; r < bb; ++r) X[r][c] = T(0);
+        X[c][c] = T(1) / S[c][c];
+        for (int r = c - 1; r >= 0; --r) {
+            T s = T(0);
+            for (int q = r + 1; q <= c; ++q) s += S[r][q] * X[q][c];
+            X[r][c] = -s / S[r][r];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < B * B; e += NTP) Di[B * B + e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
+}
+
+// the row interchanges of panel p applied (in order) to the columns right of
+// the panel, then U12 = Linv * A(p:p+bb, c)
+template <class T, int B>
+__global__ void k_u12(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p, T* __restrict__ front,
+                      const T* __restrict__ dinv, const int* __restrict__ piv) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    if (fr.nf <= p) return;
+    const int bb = min(B, fr.nf - p), F = fr.F;
+    __shared__ T Li[B][B];
+    __shared__ int pv[B];
+    const T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
+    for (int e = threadIdx.x; e < B * B; e += blockDim.x) Li[e / B][e % B] = Di[e];
+    if (threadIdx.x < bb) pv[threadIdx.x] = piv[fr.red0 + p + threadIdx.x];
+    __syncthreads();
+    const int c = p + bb + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F) return;
+    T* col = front + fr.off + int64_t(c) * F;
+    for (int jj = 0; jj < bb; ++jj) {
+        int pr = pv[jj];
+        if (pr != p + jj) {
+            T t = col[p + jj];
+            col[p + jj] = col[pr];
+            col[pr] = t;
+        }
+    }
+    T v[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) v[r] = r < bb ? col[p + r] : T(0);
+#pragma unroll
+    for (int r = B - 1; r >= 0; --r) {
+        if (r < bb) {
+            T s = v[r];
+#pragma unroll
+            for (int q = 0; q < r; ++q) s += Li[r][q] * v[q];
+            col[p + r] = s;
+        }
+    }
+}
+
+// trailing update A(p+bb:F, p+bb:F) -= L21 * U12, 64x64 tiles, 4x4 per thread
+template <class T, int B>
+__global__ void __launch_bounds__(256) k_gemm(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
+                                              T* __restrict__ front) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    if (fr.nf <= p) return;
+    const int bb = min(B, fr.nf - p), F = fr.F;
+    const int t0 = p + bb, M = F - t0;
+    if (M <= 0) return;
+    const int tiles = (M + 63) / 64;
+    if (int(blockIdx.x) >= tiles * tiles) return;
+    const int row0 = t0 + (blockIdx.x % tiles) * 64, col0 = t0 + (blockIdx.x / tiles) * 64;
+    T* A = front + fr.off;
+    __shared__ T As[B][64];
+    __shared__ T Bs[B][64];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < B * 64; e += 256) {
+        int k = e / 64, i = e % 64;
+        As[k][i] = (k < bb && row0 + i < F) ? A[int64_t(p + k) * F + row0 + i] : T(0);
+    }
+    for (int e = tid; e < B * 64; e += 256) {
+        int k = e % B, j = e / B;
+        Bs[k][j] = (k < bb && col0 + j < F) ? A[int64_t(col0 + j) * F + p + k] : T(0);
+    }
+    __syncthreads();
+    const int tx = tid % 16, ty = tid / 16;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+    for (int k = 0; k < bb; ++k) {
+        T av[4], bv[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) av[a] = As[k][tx * 4 + a];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) bv[b] = Bs[k][ty * 4 + b];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        int c = col0 + ty * 4 + b;
+        if (c >= F) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            int r = row0 + tx * 4 + a;
+            if (r < F) A[int64_t(c) * F + r] -= acc[a][b];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solve phase
+// ---------------------------------------------------------------------------
+// reduced, row-scaled rhs: wet rows minus the couplings to the eliminated
+// (dry) unknowns
+// (the solve phase works in FP64 for both factor precisions: FP32 factors are
+// read and upcast, so the accumulation error is FP64's, not FP32's)
+template <class TV>
+__global__ void k_reduce_rhs(int nred, const int* __restrict__ r2g, const char* __restrict__ isdry,
+                             const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ val,
+                             const double* __restrict__ dr, const TV* __restrict__ r, double* __restrict__ red) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nred; q += gridDim.x * blockDim.x) {
+        const int g = r2g[q];
+        double s = double(r[g]);
+        for (int e = rp[g]; e < rp[g + 1]; ++e) {
+            int c = ci[e];
+            if (isdry[c]) s -= val[e] * double(r[c]);
+        }
+        red[q] = dr[g] * s;
+    }
+}
+template <class TV>
+__global__ void k_expand(int ndim, const int* __restrict__ g2r, const double* __restrict__ dc,
+                         const double* __restrict__ red, const TV* __restrict__ r, TV* __restrict__ z) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ndim; g += gridDim.x * blockDim.x) {
+        int q = g2r[g];
+        z[g] = q >= 0 ? TV(dc[g] * red[q]) : r[g];
+    }
+}
+
+// forward elimination of one level: one CTA per front
+template <class T, int B>
+__global__ void __launch_bounds__(NT) k_fwd(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                            const int* __restrict__ child_of, const int* __restrict__ emap,
+                                            const T* __restrict__ front, const T* __restrict__ dinv,
+                                            const int* __restrict__ piv, const double* __restrict__ red,
+                                            double* __restrict__ W) {
+    const int f = lf[blockIdx.x];
+    const FrontDev fr = fronts[f];
+    const int F = fr.F, nf = fr.nf, tid = threadIdx.x;
+    double* w = W + fr.woff;
+    for (int q = tid; q < F; q += NT) w[q] = q < nf ? red[fr.red0 + q] : 0.0;
+    __syncthreads();
+    for (int s = 0; s < 2; ++s) {
+        int c = child_of[2 * f + s];
+        if (c < 0) continue;
+        const FrontDev ch = fronts[c];
+        const double* u = W + ch.woff + ch.nf;
+        const int* em = emap + ch.emap_off;
+        for (int a = tid; a < ch.nb; a += NT) w[em[a]] += u[a];
+        __syncthreads();
+    }
+    const T* A = front + fr.off;
+    __shared__ double t[B], y[B];
+    for (int p = 0; p < nf; p += B) {
+        const int bb = min(B, nf - p);
+        if (tid == 0)
+            for (int jj = 0; jj < bb; ++jj) {
+                int pr = piv[fr.red0 + p + jj];
+                if (pr != p + jj) {
+                    double tmp = w[p + jj];
+                    w[p + jj] = w[pr];
+                    w[pr] = tmp;
+                }
+            }
+        __syncthreads();
+        if (tid < bb) t[tid] = w[p + tid];
+        __syncthreads();
+        const T* Li = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
+        if (tid < bb) {
+            double s = t[tid];
+            for (int q = 0; q < tid; ++q) s += double(Li[tid * B + q]) * t[q];
+            y[tid] = s;
+            w[p + tid] = s;
+        }
+        __syncthreads();
+        for (int r = p + bb + tid; r < F; r += NT) {
+            double s = w[r];
+            for (int c = 0; c < bb; ++c) s -= double(A[int64_t(p + c) * F + r]) * y[c];
+            w[r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// backward substitution of one level: one CTA per front; warp lanes map to
+// the rows of a panel, warps split the columns.
+template <class T, int B>
+__global__ void __launch_bounds__(NT) k_bwd(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                            const int* __restrict__ vars, const T* __restrict__ front,
+                                            const T* __restrict__ dinv, double* __restrict__ W,
+                                            double* __restrict__ xred) {
+    static_assert(B <= 32, "panel must fit a warp");
+    const FrontDev fr = fronts[lf[blockIdx.x]];
+    const int F = fr.F, nf = fr.nf, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double* w = W + fr.woff;
+    const int* vv = vars + fr.voff;
+    for (int q = nf + tid; q < F; q += NT) w[q] = xred[vv[q]];
+    __syncthreads();
+    const T* A = front + fr.off;
+    __shared__ double part[NT / 32][B];
+    __shared__ double t[B];
+    const int npan = (nf + B - 1) / B;
+    for (int pi = npan - 1; pi >= 0; --pi) {
+        const int p = pi * B, bb = min(B, nf - p);
+        double s = 0.0;
+        if (lane < bb)
+            for (int c = p + bb + warp; c < F; c += NT / 32) s += double(A[int64_t(c) * F + p + lane]) * w[c];
+        part[warp][lane] = s;
+        __syncthreads();
+        if (tid < bb) {
+            double acc = w[p + tid];
+            for (int q = 0; q < NT / 32; ++q) acc -= part[q][tid];
+            t[tid] = acc;
+        }
+        __syncthreads();
+        const T* Ui = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B + B * B;
+        if (tid < bb) {
+            double x = 0.0;
+            for (int q = tid; q < bb; ++q) x += double(Ui[tid * B + q]) * t[q];
+            w[p + tid] = x;
+        }
+        __syncthreads();
+    }
+    for (int q = tid; q < nf; q += NT) xred[fr.red0 + q] = w[q];
+}
+
+__global__ void k_fill(int n, double v, double* __restrict__ a) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) a[q] = v;
+}
+
+int blocks_for(int64_t work, int per = NT) {
+    int64_t b = (work + per - 1) / per;
+    return int(std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32)));
+}
+
+}  // namespace
+
+// ===========================================================================
+// drivers
+// ===========================================================================
+NdLu::~NdLu() {
+    for (void* p : allocs) cudaFree(p);
+}
+
+template <class X>
+static X* upload(NdLu& lu, const std::vector<X>& v, cudaStream_t s) {
+    X* d = nullptr;
+    size_t bytes = sizeof(X) * std::max<size_t>(v.size(), 1);
+    if (cudaMalloc(&d, bytes) != cudaSuccess) throw EngineError(IEMIC_ERR_NOMEM);
+    lu.allocs.push_back(d);
+    if (!v.empty()) ck(cudaMemcpyAsync(d, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice, s));
+    return d;
+}
+static void* dmalloc(NdLu& lu, size_t bytes) {
+    void* d = nullptr;
+    if (cudaMalloc(&d, std::max<size_t>(bytes, 16)) != cudaSuccess) throw EngineError(IEMIC_ERR_NOMEM);
+    lu.allocs.push_back(d);
+    return d;
+}
+
+void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
+    cudaStream_t s = 0;
+    lu.prec = prec;
+    lu.plan = &plan;
+    const size_t ts = prec ? sizeof(float) : sizeof(double);
+    lu.d_fronts = upload(lu, plan.fronts, s);
+    std::vector<int> lf;
+    lu.level_start.clear();
+    for (auto& L : plan.level_fronts) {
+        lu.level_start.push_back(int(lf.size()));
+        lf.insert(lf.end(), L.begin(), L.end());
+    }
+    lu.level_start.push_back(int(lf.size()));
+    lu.d_level_fronts = upload(lu, lf, s);
+    for (int sl = 0; sl < 2; ++sl) {
+        std::vector<int> cl;
+        lu.child_start[sl].clear();
+        for (auto& L : plan.level_children[sl]) {
+            lu.child_start[sl].push_back(int(cl.size()));
+            cl.insert(cl.end(), L.begin(), L.end());
+        }
+        lu.child_start[sl].push_back(int(cl.size()));
+        lu.d_level_children[sl] = upload(lu, cl, s);
+    }
+    std::vector<int> child_of(2 * size_t(plan.nfronts), -1);
+    for (int f = 0; f < plan.nfronts; ++f) {
+        int par = plan.fronts[f].parent;
+        if (par >= 0) child_of[2 * size_t(par) + plan.child_slot[f]] = f;
+    }
+    lu.d_vars = upload(lu, plan.vars, s);
+    lu.d_emap = upload(lu, plan.emap, s);
+    lu.d_r2g = upload(lu, plan.r2g, s);
+    lu.d_g2r = upload(lu, plan.g2r, s);
+    std::vector<char> isdry(plan.ndim, 0);
+    for (int r : plan.dry_rows) isdry[r] = 1;
+    lu.d_isdry = upload(lu, isdry, s);
+    lu.d_asm_src = upload(lu, plan.asm_src, s);
+    lu.d_asm_dst = upload(lu, plan.asm_dst, s);
+    lu.d_asm_row = upload(lu, plan.asm_row, s);
+    lu.d_child_of = upload(lu, child_of, s);
+    lu.d_piv = static_cast<int*>(dmalloc(lu, sizeof(int) * size_t(std::max(plan.nred, 1))));
+    lu.d_front = dmalloc(lu, ts * size_t(plan.front_entries));
+    lu.d_dinv = dmalloc(lu, ts * size_t(plan.dinv_entries));
+    lu.d_w = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
+    lu.d_red = dmalloc(lu, sizeof(double) * size_t(std::max(plan.nred, 1)));
+    lu.d_dr = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
+    lu.d_dc = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
+    lu.d_cmax = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
+    lu.d_npert = static_cast<int*>(dmalloc(lu, sizeof(int)));
+    ck(cudaStreamSynchronize(s));
+}
+
+// Ruiz equilibration (FP64) of the wet block of J
+static void equilibrate(NdLu& lu, const int* rp, const int* ci, const double* val, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    const int nd = P.ndim, G = blocks_for(nd);
+    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dr);
+    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dc);
+    for (int it = 0; it < 3; ++it) {
+        k_rowmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dc, lu.d_dr);
+        ck(cudaMemsetAsync(lu.d_cmax, 0, sizeof(double) * nd, s));
+        k_colmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dr, lu.d_dc, lu.d_cmax);
+        k_colscale<<<G, NT, 0, s>>>(nd, lu.d_g2r, lu.d_cmax, lu.d_dc);
+    }
+}
+
+template <class T, int B>
+static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    T* front = static_cast<T*>(lu.d_front);
+    T* dinv = static_cast<T*>(lu.d_dinv);
+    const T tau = sizeof(T) == 4 ? T(1e-7) : T(1e-15);
+    equilibrate(lu, rp, ci, values, s);
+    ck(cudaMemsetAsync(front, 0, sizeof(T) * size_t(P.front_entries), s));
+    ck(cudaMemsetAsync(lu.d_npert, 0, sizeof(int), s));
+    const int64_t na = int64_t(P.asm_src.size());
+    k_assemble<T><<<blocks_for(na), NT, 0, s>>>(na, lu.d_asm_src, lu.d_asm_dst, lu.d_asm_row, ci, values, lu.d_dr,
+                                                lu.d_dc, front);
+    for (int h = 0; h < P.nlevels; ++h) {
+        const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+        const int* lf = lu.d_level_fronts + lu.level_start[h];
+        for (int sl = 0; sl < 2; ++sl) {
+            int nc = lu.child_start[sl][h + 1] - lu.child_start[sl][h];
+            if (nc == 0) continue;
+            int64_t mx = 0;
+            for (int c : P.level_children[sl][h]) mx = std::max<int64_t>(mx, int64_t(P.fronts[c].nb) * P.fronts[c].nb);
+            dim3 g(blocks_for(mx), nc);
+            k_extend_add<T><<<g, NT, 0, s>>>(lu.d_fronts, lu.d_level_children[sl] + lu.child_start[sl][h], lu.d_emap,
+                                             front);
+        }
+        const int maxnf = P.level_maxnf[h], maxF = P.level_maxF[h];
+        for (int p = 0; p < maxnf; p += B) {
+            k_panel<T, B><<<nfr, NTP, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert);
+            const int rest = maxF - p;
+            dim3 g1((rest + NT - 1) / NT, nfr);
+            k_u12<T, B><<<g1, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv);
+            const int tiles = (rest + 63) / 64;
+            dim3 g2(tiles * tiles, nfr);
+            k_gemm<T, B><<<g2, 256, 0, s>>>(lu.d_fronts, lf, p, front);
+        }
+    }
+    ck(cudaGetLastError());
+    ck(cudaMemcpyAsync(&lu.npert, lu.d_npert, sizeof(int), cudaMemcpyDeviceToHost, s));
+    lu.factored = true;
+}
+
+void ndlu_factor(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {
+    if (lu.prec) factor_t<float, 32>(lu, rp, ci, values, s);
+    else factor_t<double, 32>(lu, rp, ci, values, s);
+}
+
+template <class T, int B, class TV>
+static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, const TV* r, TV* z, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    double* red = static_cast<double*>(lu.d_red);
+    double* W = static_cast<double*>(lu.d_w);
+    const T* front = static_cast<const T*>(lu.d_front);
+    const T* dinv = static_cast<const T*>(lu.d_dinv);
+    k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red);
+    for (int h = 0; h < P.nlevels; ++h) {
+        const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+        k_fwd<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lu.d_level_fronts + lu.level_start[h], lu.d_child_of, lu.d_emap,
+                                       front, dinv, lu.d_piv, red, W);
+    }
+    for (int h = P.nlevels - 1; h >= 0; --h) {
+        const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+        k_bwd<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lu.d_level_fronts + lu.level_start[h], lu.d_vars, front, dinv, W,
+                                       red);
+    }
+    k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_dc, red, r, z);
+    ck(cudaGetLastError());
+}
+
+void ndlu_apply(NdLu& lu, const int* rp, const int* ci, const double* values, const void* r, void* z, int vec_fp32,
+                cudaStream_t s) {
+    if (!lu.factored) throw EngineError(IEMIC_ERR_STATE);
+    if (lu.prec) {
+        if (vec_fp32)
+            apply_t<float, 32, float>(lu, rp, ci, values, static_cast<const float*>(r), static_cast<float*>(z), s);
+        else
+            apply_t<float, 32, double>(lu, rp, ci, values, static_cast<const double*>(r), static_cast<double*>(z), s);
+    } else {
+        if (vec_fp32)
+            apply_t<double, 32, float>(lu, rp, ci, values, static_cast<const float*>(r), static_cast<float*>(z), s);
+        else
+            apply_t<double, 32, double>(lu, rp, ci, values, static_cast<const double*>(r), static_cast<double*>(z), s);
+    }
+}
+
+}  // namespace iemic

@@ -1,0 +1,85 @@
+// Nested-dissection multilevel block LU of the THCM Jacobian (preconditioner).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+namespace iemic {
+
+// One frontal matrix of the elimination tree: `nf` own ("fully summed")
+// unknowns followed by `nb` boundary unknowns owned by ancestors.
+struct FrontDev {
+    int nf, nb, F;          // F = nf + nb, leading dimension of the dense front
+    int parent;             // -1 at the root
+    int red0;               // reduced index of the first own unknown
+    int pad_;
+    int64_t off;            // offset of the column-major F x F front
+    int64_t voff;           // offset into `vars` (F reduced indices)
+    int64_t dinv_off;       // offset of the per-panel inverse diagonal blocks
+    int64_t emap_off;       // offset into `emap` (nb parent-local indices)
+    int64_t woff;           // offset of the front's solve vector (F entries)
+};
+
+// Host-side symbolic analysis, built once per land mask.
+struct NdPlan {
+    int ndim = 0, nred = 0, nfronts = 0, nlevels = 0, panel = 32;
+    std::vector<FrontDev> fronts;
+    std::vector<std::vector<int>> level_fronts;   // fronts by height (leaves first)
+    std::vector<int> level_maxnf, level_maxF;
+    std::vector<std::vector<int>> level_children[2];   // per level, children in slot s of its fronts
+    std::vector<int> r2g, g2r;      // reduced <-> global unknown
+    std::vector<int> vars;          // per front: reduced indices of its F unknowns
+    std::vector<int> emap;          // per front: parent-local index of its nb boundary unknowns
+    std::vector<int> child_slot;    // slot of each front in its parent
+    std::vector<int> dry_rows;      // unknowns the factorisation leaves out (identity rows, pins)
+    std::vector<int> pins;          // pinned pressure unknowns
+    std::vector<int> asm_src;       // CSR entry index
+    std::vector<int> asm_row;       // its row
+    std::vector<int64_t> asm_dst;   // offset in the front storage
+    int64_t front_entries = 0, dinv_entries = 0, emap_entries = 0, w_entries = 0;
+    double flops = 0.0;             // factorisation flop count
+    int64_t factor_entries = 0;     // entries the solve phase reads
+};
+
+void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::vector<int>& landm,
+                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel);
+
+// Device-resident factorisation for one precision.
+struct NdLu {
+    int prec = 0;   // 0 FP64, 1 FP32
+    const NdPlan* plan = nullptr;
+    // device copies of the plan
+    FrontDev* d_fronts = nullptr;
+    int* d_level_fronts = nullptr;          // concatenated per level
+    std::vector<int> level_start;           // offsets into d_level_fronts
+    int* d_level_children[2] = {nullptr, nullptr};
+    std::vector<int> child_start[2];
+    int *d_vars = nullptr, *d_emap = nullptr, *d_r2g = nullptr, *d_g2r = nullptr, *d_child_of = nullptr;
+    char* d_isdry = nullptr;                // 1 for unknowns left out of the factorisation
+    int* d_asm_src = nullptr;
+    int* d_asm_row = nullptr;
+    double *d_dr = nullptr, *d_dc = nullptr, *d_cmax = nullptr;   // equilibration scalings
+    int64_t* d_asm_dst = nullptr;
+    int* d_piv = nullptr;                   // per reduced unknown: block-local pivot source
+    void* d_front = nullptr;                // front storage (T)
+    void* d_dinv = nullptr;                 // inverse diagonal panel blocks (T)
+    void* d_w = nullptr;                    // solve vectors (T)
+    void* d_red = nullptr;                  // reduced rhs / solution (T)
+    int* d_npert = nullptr;                 // perturbed-pivot counter
+    int npert = 0;
+    bool factored = false;
+    std::vector<void*> allocs;
+    ~NdLu();
+};
+
+void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec);
+// values: FP64 CSR values of J (equilibrated in FP64, then cast to the factor precision)
+void ndlu_factor(NdLu& lu, const int* row_ptr, const int* col_idx, const double* values, cudaStream_t s);
+// z = M^{-1} r on global-indexed vectors (float if vec_fp32, else double);
+// `values` are the FP64 CSR values (used for the eliminated columns). The
+// triangular solves accumulate in FP64 whatever the factor precision.
+void ndlu_apply(NdLu& lu, const int* row_ptr, const int* col_idx, const double* values, const void* r, void* z,
+                int vec_fp32, cudaStream_t s);
+
+}  // namespace iemic

@@ -350,7 +350,7 @@ void Engine::jacobian_dev(const double* x) {
     launch_jacobian(geo, P, pat, d_al, d_pads, d_val, d_val32, stream);
     ck(cudaGetLastError());
     jac_valid = true;
-    fact_stale = true;
+    fact64_stale = fact32_stale = true;
 }
 
 // ---------------------------------------------------------------------------

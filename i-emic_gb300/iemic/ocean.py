@@ -52,11 +52,13 @@ class Config(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("restart", ctypes.c_int), ("max_iters", ctypes.c_int),
                 ("tol", ctypes.c_double), ("max_refinements", ctypes.c_int),
-                ("inner_tol", ctypes.c_double), ("transpose", ctypes.c_int)]
+                ("inner_tol", ctypes.c_double), ("transpose", ctypes.c_int),
+                ("reuse_preconditioner", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
-    _fields_ = [("iters", ctypes.c_int), ("refinements", ctypes.c_int), ("relres", ctypes.c_double),
+    _fields_ = [("iters", ctypes.c_int), ("factorizations", ctypes.c_int), ("perturbed_pivots", ctypes.c_int),
+                ("refinements", ctypes.c_int), ("relres", ctypes.c_double),
                 ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
 
 
@@ -277,6 +279,7 @@ class Ocean:
         st = SolveStats()
         rc = self.L.iemic_solve(self._h, _dp(b), _dp(x), ctypes.byref(o), ctypes.byref(st))
         stats = dict(iters=st.iters, refinements=st.refinements, relres=st.relres,
+                     factorizations=st.factorizations, perturbed_pivots=st.perturbed_pivots,
                      time_factor_ms=st.time_factor_ms, time_solve_ms=st.time_solve_ms, status=rc)
         if rc not in (0, -3):
             raise IemicError(rc, "solve")

@@ -104,9 +104,14 @@ typedef struct {
     int max_refinements;   /* outer FP64 refinement steps (mixed only) */
     double inner_tol;      /* FP32 inner relative tolerance (mixed only) */
     int transpose;         /* 0: J x = b, 1: J^T x = b (adjoint solve) */
+    int reuse_preconditioner; /* 0: refactor when J changed since the last factorisation;
+                                 1: keep the existing factorisation (the reference recomputes its
+                                 preconditioner once per continuation step, Ocean::preProcess) */
 } iemic_solve_opts;
 typedef struct {
     int iters;             /* total inner Krylov iterations */
+    int factorizations;    /* preconditioner (re)builds performed by this call */
+    int perturbed_pivots;  /* pivots the last factorisation had to perturb */
     int refinements;       /* outer refinement steps */
     double relres;         /* final FP64 ||b - J x|| / ||b|| */
     double time_factor_ms; /* time spent (re)building the preconditioner */
