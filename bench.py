@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""Newton steps/s of the THCM ocean continuation on one GB300.
+
+Workload (default ``global_96x38x12``): the 4-degree global ocean, 96x38x12
+cells with a seeded land mask (about 30% land, periodic in longitude), 262,656
+unknowns. A steady state at Combined Forcing ``--setup-comb`` is computed first
+(untimed); then ``--warmup`` pseudo-arclength continuation steps in the
+freshwater forcing ("Salinity Forcing", par 15) run untimed and ``--steps``
+steps are timed, first on the mixed path (FP32 factors, FP64 GMRES and
+Newton: IEMIC_PREC_MIXED), then from the same point on the plain FP64 path.
+Every linear solve reaches ||b - J x|| <= 1e-8 ||b|| and every corrector
+||F(x)||_2 <= 1e-8 ||F(0)||_2 (the reference's residual test 'R').
+
+A "step" is one continuation step (predictor plus Newton corrector); the
+metric counts Newton corrector iterations (one Jacobian, three residuals,
+one preconditioner rebuild, two solves and the update each) per second of
+device time. ``--impl reference`` times the CPU restatement of the same
+Newton iteration (C++ oracle assembly + numpy/LAPACK multifrontal LU) on the
+host cores; it is the CPU baseline, not the target.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "i-emic_gb300"))
+
+METRIC = "Newton steps/s, 96×38×12 ocean, to 1e-8 residual: FP32+refine vs FP64 GPU"
+UNIT = "Newton steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="global_96x38x12", choices=["global_96x38x12", "box_16x16x4"])
+    ap.add_argument("--setup-comb", type=float, default=0.1)
+    ap.add_argument("--fp64-steps", type=int, default=None, help="continuation steps of the FP64 comparison")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-iters", type=int, default=1, help="Newton iterations of the CPU sample")
+    return ap.parse_args()
+
+
+def workload(name):
+    from iemic import workloads as W
+    if name == "global_96x38x12":
+        cfg = W.global_96x38x12()
+        return cfg, W.seeded_global_mask(cfg, 0), None
+    cfg = W.box_16x16x4()
+    return cfg, None, W.box_forcing(cfg)
+
+
+def continuation_opts(ocean, precision, steps, fscale):
+    """Freshwater-forcing continuation: the step sizes and Newton limits of the
+    reference's parameterfiles/continuation_params.xml, residual test 'R'."""
+    return ocean.default_continuation_opts("Salinity Forcing", precision), dict(
+        ds=0.01, ds_min=1e-8, ds_max=0.1, destination=10.0, max_steps=steps, max_newton=15, min_newton=1,
+        opt_newton=4.0, newton_tol=1e-8 * fscale, residual_test=b"R", normalize=b"N", tangent=b"S",
+        predictor_bound=1e30, tan_scaling=1.0)
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier_max(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier_sum(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            if dev.isdigit() and f[0] != dev and len(set(l.split(",")[0] for l in out.splitlines())) > 1:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def roofline(stats, peaks):
+    """Roofline of the dominant instrumented kernel class in the timed region."""
+    name, s = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    avg_ms = s["ms"] / max(s["launches"], 1)
+    out = {"kernel": name, "launches": s["launches"], "avg_launch_ms": avg_ms}
+    if name == "factor_gemm":
+        # FP32 (or FP64) SIMT GEMM: no measured SIMT peak exists; nominal FP32 rate
+        peak = 2 * 128 * 152 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        ach = s["flops"] / max(s["launches"], 1) / (avg_ms * 1e-3) / 1e12
+        out.update(bound="fp32_simt", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak,
+                   peak_source="nominal FP32 SIMT (152 SMs x 128 FMA/clk x max clock)")
+    else:
+        peak = peaks.get("hbm_gbs", 6800.0)
+        ach = s["bytes"] / max(s["launches"], 1) / (avg_ms * 1e-3) / 1e9
+        out.update(bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak,
+                   peak_source="measured" if "hbm_gbs" in peaks else "fallback")
+    out["algorithmic_bytes_per_launch"] = s["bytes"] / max(s["launches"], 1)
+    out["traffic"] = None
+    tf = os.path.join(REPO, "profiles", "traffic_%s.json" % name)
+    if os.path.exists(tf):
+        try:
+            with open(tf) as fh:
+                out["traffic"] = json.load(fh).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            pass
+    out["classes"] = {k: {"ms": v["ms"], "launches": v["launches"]} for k, v in stats.items()}
+    return out
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's Newton iteration on the host cores
+# ---------------------------------------------------------------------------
+def cpu_newton_sample(cfg, lm, frc, iters, par_setup):
+    """One (or more) Newton corrector iterations on the CPU: oracle assembly of
+    J and F (plus F(par+eps) for dF/dpar), FP64 multifrontal LU, two solves and
+    the update, from the seeded rest state at the workload's parameters."""
+    import oracle
+    from oracle.multifrontal import Factorization, Plan
+    from iemic import workloads as W
+    o = oracle.Oracle(cfg, lm)
+    if frc:
+        o.set_forcing(**frc)
+    names = {"Combined Forcing": "COMB", "Temperature Forcing": "TEMP", "Salinity Forcing": "SALT",
+             "Wind Forcing": "WIND"}
+    for name, v in W.STARTING_PARAMETERS:
+        o.set_par(names[name], v)
+    o.set_par("COMB", par_setup)
+    plan = Plan(o.landm(), cfg["n"], cfg["m"], cfg["l"], cfg["periodic"])
+    rp, ci = o.graph()
+    x = W.rest_state_with_ts_noise(cfg, 0)
+    eps = 1e-5
+    salt = o.get_par("SALT")
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        F = o.rhs(x)
+        o.set_par("SALT", salt + eps)
+        dfdp = (o.rhs(x) - F) / eps
+        o.set_par("SALT", salt)
+        vals, _ = o.jacobian(x)
+        fact = Factorization(plan, rp, ci, vals)
+        fact.solve(dfdp)            # J y = dF/dpar (the bordered corrector's second solve)
+        x = x + fact.solve(-F)
+    dt = time.perf_counter() - t0
+    o.close()
+    threads = os.cpu_count()
+    return {"value": iters / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d Newton iteration(s) at %s: oracle assembly (J, F, F(par+eps)) + FP64 multifrontal LU "
+                      "(numpy/OpenBLAS, %d threads) + 2 exact solves; %.1f s" % (iters, "C2" if cfg["n"] == 96
+                                                                                   else "box", threads, dt)}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cfg, lm, frc = workload(args.workload)
+    k = max(1, min(args.steps, 2))
+    base = cpu_newton_sample(cfg, lm, frc, k, args.setup_comb)
+    line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": k,
+            "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded land mask and state)",
+            "config": {"workload": args.workload, "grid": [cfg["n"], cfg["m"], cfg["l"]],
+                       "continuation_parameter": "Salinity Forcing", "tolerance": 1e-8},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import ctypes
+
+    import torch
+    from iemic import Ocean, load_library
+    from iemic import workloads as W
+    from iemic.ocean import ContinuationStats, _asdict
+
+    torch.cuda.init()
+    L = load_library()
+    cfg, lm, frc = workload(args.workload)
+    oc = Ocean(cfg, lm, forcing=frc, starting_parameters=W.STARTING_PARAMETERS)
+    nd = oc.ndim
+    fscale = float(np.linalg.norm(oc.computeRHS(np.zeros(nd))))
+    stream = torch.cuda.ExternalStream(oc.stream())
+
+    # --- setup (untimed): steady state at Combined Forcing = setup_comb
+    oc.setPar("Combined Forcing", 0.0)
+    x0, st0 = oc.continuation(np.zeros(nd), par="Combined Forcing", precision=1, ds=args.setup_comb / 2,
+                              ds_max=args.setup_comb, destination=args.setup_comb, max_steps=20,
+                              newton_tol=1e-8 * fscale, residual_test=b"R", predictor_bound=1e30)
+    if st0["status"] != 0 or not st0["reached_destination"]:
+        raise RuntimeError("setup continuation failed: %s" % st0)
+
+    def cont_dev(x_dev, precision, steps):
+        o, kw = continuation_opts(oc, precision, steps, fscale)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        st = ContinuationStats()
+        rc = L.iemic_continuation_run_dev(oc.handle, ctypes.c_void_p(x_dev.data_ptr()), ctypes.byref(o),
+                                          ctypes.byref(st))
+        s = _asdict(st)
+        s["status"] = rc
+        if rc != 0:
+            raise RuntimeError("continuation failed: %s" % s)
+        return s
+
+    # --- warm-up: W continuation steps in the freshwater forcing (mixed path)
+    salt0 = oc.getPar("Salinity Forcing")
+    xw = torch.tensor(x0, dtype=torch.float64, device="cuda")
+    if args.warmup > 0:
+        cont_dev(xw, 1, args.warmup)
+    par_w = oc.getPar("Salinity Forcing")
+    x_start = xw.clone()
+
+    peaks = load_peaks()
+    info = oc.solverInfo()
+    results = {}
+    for label, prec, steps in (("mixed", 1, args.steps), ("fp64", 0, args.fp64_steps or args.steps)):
+        x = x_start.clone()
+        oc.setPar("Salinity Forcing", par_w)
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        timing = label == "mixed"
+        if timing:
+            oc.kernelTiming(True)
+            clocks = Clocks()
+            n0 = L.iemic_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st = cont_dev(x, prec, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if timing:
+            launches = L.iemic_launch_count() - n0
+            clk = clocks.stop()
+            kstats = oc.kernelStats()
+            oc.kernelTiming(False)
+        ms = barrier_max(ms, world)
+        iters = barrier_sum(st["newton_iters"], world)
+        results[label] = dict(ms=ms, newton_iters=iters, stats=st, value=iters / (ms * 1e-3))
+        if timing:
+            results[label].update(launches=launches, clocks=clk, kstats=kstats)
+
+    # --- end to end through the public API with host buffers (mixed path)
+    xh = x_start.cpu().numpy()
+    oc.setPar("Salinity Forcing", par_w)
+    o, kw = continuation_opts(oc, 1, args.steps, fscale)
+    kw["par"] = "Salinity Forcing"
+    kw["precision"] = 1
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, ste = oc.continuation(xh, **kw)
+    e2e_s = time.perf_counter() - t0
+    e2e_iters = barrier_sum(ste["newton_iters"], world)
+    e2e_s = barrier_max(e2e_s, world)
+
+    if rank != 0:
+        return
+    mixed, fp64 = results["mixed"], results["fp64"]
+    line = {
+        "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 factors / f64 Krylov+Newton",
+        "data": "synthetic (seeded land mask, idealized forcing)",
+        "config": {"workload": args.workload, "grid": [cfg["n"], cfg["m"], cfg["l"]], "unknowns": nd,
+                   "continuation_parameter": "Salinity Forcing", "setup_combined_forcing": args.setup_comb,
+                   "start_salinity_forcing": par_w, "initial_salinity_forcing": salt0,
+                   "linear_tol": 1e-8, "newton_tol_abs": 1e-8 * fscale, "parallelism": "replicas",
+                   "l2": "working set larger than L2: FP32 factors of %.2f GB read per preconditioner apply"
+                         % (4e-9 * info["factor_entries"]),
+                   "factor_gflop": info["factor_flops"] / 1e9, "fronts": info["fronts"]},
+        "newton_iters": mixed["newton_iters"], "continuation": {k: mixed["stats"][k] for k in (
+            "steps", "failed_steps", "linear_solves", "krylov_iters", "factorizations", "par",
+            "time_assembly_ms", "time_factor_ms", "time_solve_ms")},
+        "fp64_gpu": {"value": fp64["value"], "ms": fp64["ms"], "newton_iters": fp64["newton_iters"],
+                     "steps": fp64["stats"]["steps"], "krylov_iters": fp64["stats"]["krylov_iters"],
+                     "time_factor_ms": fp64["stats"]["time_factor_ms"],
+                     "time_solve_ms": fp64["stats"]["time_solve_ms"]},
+        "speedup_vs_fp64_gpu": mixed["value"] / fp64["value"],
+        "e2e": {"value": e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * nd / args.steps,
+                "d2h_bytes_per_step": 8 * nd / args.steps,
+                "note": "one continuation call of %d steps with the state in host memory" % args.steps},
+        "gpu_launches": mixed["launches"],
+        "clocks": mixed["clocks"],
+        "roofline": roofline(mixed["kstats"], peaks),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_newton_sample(cfg, lm, frc, args.cpu_iters, args.setup_comb)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

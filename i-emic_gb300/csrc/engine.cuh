@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/iemic_gb300.h"
+#include "ktimer.cuh"
 #include "ocean_impl.cuh"
 
 namespace iemic {
@@ -59,6 +60,7 @@ struct Engine {
     NdLu* lu32 = nullptr;
     Krylov* kry = nullptr;
     std::vector<int> h_col;   // host copy of the CSR column indices
+    KTimer timer;             // optional per-kernel-class device timing
 
     ~Engine();
     void init(const iemic_config& c, const int* landm_in);

@@ -11,9 +11,14 @@
 // into one sweep over the basis and the update into a second sweep. The
 // Hessenberg least-squares problem (Givens rotations) is solved in FP64.
 //
-// Mixed precision (IEMIC_PREC_MIXED): J, the factorisation, the Krylov basis
-// and all inner products are FP32. The residual r = b - J x, the solution
-// update and the convergence test stay FP64 (outer iterative refinement).
+// Mixed precision (IEMIC_PREC_MIXED): the factorisation is computed and
+// stored in FP32 (half the bytes, FP32 GEMM rate); its triangular solves
+// accumulate in FP64 and GMRES, J and the convergence test are FP64. This is
+// GMRES-based iterative refinement with a low-precision factorisation
+// (Carson & Higham, SIAM J. Sci. Comput. 40 (2018) A817). The all-FP32 inner
+// Krylov variant (IEMIC_PREC_FP32_KRYLOV: J, basis and inner products in FP32,
+// FP64 residual refinement outside) stalls on the 96x38x12 ocean, whose
+// Jacobian has a condition number near 1e8, and is kept as an option only.
 //
 // SpMV: rows hold 7..24 entries, so four lanes share a row and reduce with
 // warp shuffles; a warp covers eight consecutive rows (contiguous loads of
@@ -157,10 +162,10 @@ int spmv_grid(int nrows) {
 }  // namespace
 
 void launch_spmv64(int nrows, const int* rp, const int* ci, const double* v, const double* x, double* y, cudaStream_t s) {
-    spmv_csr4<double><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y);
+    spmv_csr4<double><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y); IEMIC_COUNT_LAUNCH();
 }
 void launch_spmv32(int nrows, const int* rp, const int* ci, const float* v, const float* x, float* y, cudaStream_t s) {
-    spmv_csr4<float><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y);
+    spmv_csr4<float><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y); IEMIC_COUNT_LAUNCH();
 }
 
 // Krylov workspace (both precisions share the layout)
@@ -266,25 +271,20 @@ void Engine::build_preconditioner(int precision) {
     if (!lu) {
         lu = new NdLu();
         ndlu_setup(*lu, *ndplan, precision == IEMIC_PREC_MIXED ? 1 : 0);
+        lu->timer = &timer;
     }
     ndlu_factor(*lu, d_rowptr, d_col, d_val, stream);
     ck(cudaStreamSynchronize(stream));
+    timer.drain();
     if (precision == IEMIC_PREC_MIXED) fact32_stale = false; else fact64_stale = false;
 }
 
 void Engine::apply_precon(int precision, const double* v, double* out) {
     NdLu* lu = lu_for(precision);
     if (!lu || !lu->factored) throw EngineError(IEMIC_ERR_STATE);
-    if (precision == IEMIC_PREC_MIXED) {
-        ensure_krylov(*this, kry ? kry->m : 100, 1);
-        float* w = static_cast<float*>(kry->w);
-        float* z = static_cast<float*>(kry->z);
-        convert<double, float><<<vgrid(ndim), 256, 0, stream>>>(ndim, v, w, 1.0);
-        ndlu_apply(*lu, d_rowptr, d_col, d_val, w, z, 1, stream);
-        convert<float, double><<<vgrid(ndim), 256, 0, stream>>>(ndim, z, out, 1.0);
-    } else {
-        ndlu_apply(*lu, d_rowptr, d_col, d_val, v, out, 0, stream);
-    }
+    // FP64 vectors in and out for both factor precisions (the mixed solve
+    // applies its FP32 factors to FP64 Krylov vectors the same way)
+    ndlu_apply(*lu, d_rowptr, d_col, d_val, v, out, 0, stream);
     ck(cudaGetLastError());
 }
 
@@ -302,13 +302,15 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
     T* z = static_cast<T*>(K.z);
     const int G = vgrid(n);
     auto dot = [&](const T* a, const T* c) {
-        multidot<T><<<G, 256, 0, s>>>(n, 1, a == c ? a : a, c, K.part);
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+        multidot<T><<<G, 256, 0, s>>>(n, 1, a == c ? a : a, c, K.part); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
         ck(cudaMemcpyAsync(K.hpin, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
         ck(cudaStreamSynchronize(s));
         return K.hpin[0];
     };
     std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    // CSR values + column indices + row pointers, x gathered once, y written
+    const double spmv_bytes = double(e.nnz) * (sizeof(T) + 4) + 4.0 * (n + 1) + 2.0 * sizeof(T) * n;
     ck(cudaMemsetAsync(x, 0, sizeof(T) * n, s));
     const double beta0 = std::sqrt(dot(b, b));
     if (!(beta0 > 0.0)) {
@@ -324,33 +326,37 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
         if (first) {
             ck(cudaMemcpyAsync(w, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
         } else {
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, x, z);
-            sub_from<T><<<G, 256, 0, s>>>(n, b, z, w);
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, x, z); IEMIC_COUNT_LAUNCH();
+            sub_from<T><<<G, 256, 0, s>>>(n, b, z, w); IEMIC_COUNT_LAUNCH();
         }
         first = false;
         const double beta = std::sqrt(dot(w, w));
         if (!std::isfinite(beta)) throw EngineError(IEMIC_ERR_NAN);
         relres = beta / beta0;
         if (relres <= tol || it >= maxit) break;
-        scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / beta, V);
+        scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / beta, V); IEMIC_COUNT_LAUNCH();
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         int j = 0;
         for (; j < m && it < maxit;) {
             ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, V + size_t(j) * n, z, sizeof(T) == 4, s);
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, z, w);
+            cudaEvent_t ev = e.timer.start(s);
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, z, w); IEMIC_COUNT_LAUNCH();
+            e.timer.stop(ev, s, IEMIC_KC_SPMV, spmv_bytes, 2.0 * double(e.nnz));
             for (int pass = 0; pass < 2; ++pass) {   // CGS2
-                multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part);
-                reduce_parts<<<1, 256, 0, s>>>(G, j + 1, K.part, K.dots, K.h, pass == 0);
-                basis_update<T><<<G, 256, 0, s>>>(n, j + 1, V, K.dots, w);
+                multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
+                reduce_parts<<<1, 256, 0, s>>>(G, j + 1, K.part, K.dots, K.h, pass == 0); IEMIC_COUNT_LAUNCH();
+                basis_update<T><<<G, 256, 0, s>>>(n, j + 1, V, K.dots, w); IEMIC_COUNT_LAUNCH();
             }
-            multidot<T><<<G, 256, 0, s>>>(n, 1, w, w, K.part);
-            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0);
+            multidot<T><<<G, 256, 0, s>>>(n, 1, w, w, K.part); IEMIC_COUNT_LAUNCH();
+            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0); IEMIC_COUNT_LAUNCH();
             ck(cudaMemcpyAsync(K.hpin, K.h, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, s));
             ck(cudaStreamSynchronize(s));
             const double hn = std::sqrt(K.hpin[j + 1]);
             if (!std::isfinite(hn)) throw EngineError(IEMIC_ERR_NAN);
-            if (hn > 0.0) scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / hn, V + size_t(j + 1) * n);
+            if (hn > 0.0) {
+                scale_by<T><<<G, 256, 0, s>>>(n, w, 1.0 / hn, V + size_t(j + 1) * n); IEMIC_COUNT_LAUNCH();
+            }
             for (int i = 0; i <= j; ++i) H[size_t(i) * m + j] = K.hpin[i];
             H[size_t(j + 1) * m + j] = hn;
             for (int i = 0; i < j; ++i) {   // apply the previous Givens rotations
@@ -378,9 +384,9 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
             y[i] = sum / H[size_t(i) * m + i];
         }
         ck(cudaMemcpyAsync(K.y, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
-        combine<T><<<G, 256, 0, s>>>(n, j, V, K.y, w);
+        combine<T><<<G, 256, 0, s>>>(n, j, V, K.y, w); IEMIC_COUNT_LAUNCH();
         ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, w, z, sizeof(T) == 4, s);
-        add_to<T><<<G, 256, 0, s>>>(n, z, x);
+        add_to<T><<<G, 256, 0, s>>>(n, z, x); IEMIC_COUNT_LAUNCH();
         ck(cudaStreamSynchronize(s));   // y is a host temporary
     }
     ck(cudaGetLastError());
@@ -391,7 +397,10 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
 int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
     if (!jac_valid) return IEMIC_ERR_STATE;
     if (o.transpose) return solve_transpose_dev(b, x, o, st);
-    const int prec = o.precision == IEMIC_PREC_MIXED ? IEMIC_PREC_MIXED : IEMIC_PREC_FP64;
+    // IEMIC_PREC_MIXED: FP32 factors under an FP64 Krylov solve;
+    // IEMIC_PREC_FP32_KRYLOV: FP32 factors and FP32 GMRES inside FP64 refinement
+    const bool fp32_krylov = o.precision == IEMIC_PREC_FP32_KRYLOV;
+    const int prec = o.precision == IEMIC_PREC_FP64 ? IEMIC_PREC_FP64 : IEMIC_PREC_MIXED;
     auto t0 = std::chrono::steady_clock::now();
     ensure_solver();
     NdLu*& lu = lu_for(prec);
@@ -403,14 +412,14 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     st.perturbed_pivots = lu->npert;
     auto t1 = std::chrono::steady_clock::now();
     st.time_factor_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
-    ensure_krylov(*this, o.restart, prec);
+    ensure_krylov(*this, o.restart, fp32_krylov ? 1 : 0);
     Krylov& K = *kry;
     const int n = ndim;
     const int G = vgrid(n);
     cudaStream_t s = stream;
     // ||b||
-    multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part);
-    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+    multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double bn2 = 0.0;
     ck(cudaMemcpyAsync(&bn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
     ck(cudaStreamSynchronize(s));
@@ -423,14 +432,14 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     }
     int rc = IEMIC_OK;
     double relres = 1.0;
-    if (prec == IEMIC_PREC_FP64) {
-        scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64);
+    if (!fp32_krylov) {
+        scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
         double est = 1.0;
         st.iters += gmres<double>(*this, *lu, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est);
-        axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x);
-        residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64);
-        multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part);
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+        axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
+        residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+        multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
         double rn2 = 0.0;
         ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
         ck(cudaStreamSynchronize(s));
@@ -446,14 +455,14 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
             if (!std::isfinite(relres)) return IEMIC_ERR_NAN;
             if (relres <= o.tol) break;
             if (ref >= o.max_refinements || st.iters >= o.max_iters) break;
-            convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm);
+            convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm); IEMIC_COUNT_LAUNCH();
             double est = 1.0;
             double inner = std::max(o.inner_tol, 0.5 * o.tol / relres);
             st.iters += gmres<float>(*this, *lu, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner, &est);
-            axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x);
-            residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64);
-            multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part);
-            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0);
+            axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x); IEMIC_COUNT_LAUNCH();
+            residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+            multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
+            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
             double rn2 = 0.0;
             ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
             ck(cudaStreamSynchronize(s));
@@ -462,6 +471,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
         }
     }
     st.relres = relres;
+    timer.drain();
     auto t2 = std::chrono::steady_clock::now();
     st.time_solve_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
     if (relres > o.tol) rc = IEMIC_ERR_NOT_CONVERGED;
@@ -472,4 +482,52 @@ int Engine::solve_transpose_dev(const double*, double*, const iemic_solve_opts&,
     return IEMIC_ERR_STATE;
 }
 
+}  // namespace iemic
+
+// ---------------------------------------------------------------------------
+// small device-vector helpers for the Newton / continuation drivers
+// ---------------------------------------------------------------------------
+namespace iemic {
+namespace {
+__global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) y[r] = a * x[r] + b * y[r];
+}
+}  // namespace
+double dev_dot(Engine& e, const double* a, const double* b) {
+    ensure_krylov(e, e.kry ? e.kry->m : 100, e.kry ? e.kry->prec : 0);
+    const int n = e.ndim, G = vgrid(n);
+    multidot<double><<<G, 256, 0, e.stream>>>(n, 1, a, b, e.kry->part); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, 32, 0, e.stream>>>(G, 1, e.kry->part, e.kry->dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    double v = 0.0;
+    ck(cudaMemcpyAsync(&v, e.kry->dots, sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+    ck(cudaStreamSynchronize(e.stream));
+    return v;
+}
+__global__ void k_absmax_part(int n, const double* __restrict__ x, double* __restrict__ part) {
+    double m = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) m = fmax(m, fabs(x[r]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double sm[32];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (blockDim.x >> 5); ++w) m = fmax(m, sm[w]);
+        part[blockIdx.x] = m;
+    }
+}
+double dev_norm_inf(Engine& e, const double* a) {
+    ensure_krylov(e, e.kry ? e.kry->m : 100, e.kry ? e.kry->prec : 0);
+    const int G = vgrid(e.ndim);
+    k_absmax_part<<<G, 256, 0, e.stream>>>(e.ndim, a, e.kry->part); IEMIC_COUNT_LAUNCH();
+    std::vector<double> h(size_t(G), 0.0);
+    ck(cudaMemcpyAsync(h.data(), e.kry->part, sizeof(double) * G, cudaMemcpyDeviceToHost, e.stream));
+    ck(cudaStreamSynchronize(e.stream));
+    double m = 0.0;
+    for (double v : h) m = std::max(m, v);
+    return m;
+}
+void dev_axpby(Engine& e, double a, const double* x, double b, double* y) {
+    k_axpby<<<vgrid(e.ndim), 256, 0, e.stream>>>(e.ndim, a, x, b, y); IEMIC_COUNT_LAUNCH();
+    ck(cudaGetLastError());
+}
 }  // namespace iemic

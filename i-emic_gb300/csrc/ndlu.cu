@@ -27,6 +27,7 @@
 
 #include "engine.cuh"
 #include "ndlu.cuh"
+#include "ktimer.cuh"
 #include "stencil.cuh"
 
 namespace iemic {
@@ -422,87 +423,82 @@ __global__ void k_extend_add(const FrontDev* __restrict__ fronts, const int* __r
     }
 }
 
-// Panel p of every front of a level: LU with partial pivoting over all the
-// front's fully-summed rows [j, nf) for columns p..p+bb-1, applied to the
-// whole panel height (this also yields L21 for the boundary rows). Then the
-// inverses of the diagonal block's unit-lower and upper factors are stored for
-// the U12 update and the solve phase.
+// Panel p of every front of a level: LU with partial pivoting inside the
+// bb x bb diagonal block (block-local pivoting), plus the inverses of its
+// unit-lower and upper factors. With the barotropic pressures deferred to the
+// root, no fully-summed block is singular and local pivots suffice.
 template <class T, int B>
-__global__ void __launch_bounds__(NTP) k_panel(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
-                                               T* __restrict__ front, T* __restrict__ dinv, int* __restrict__ piv,
-                                               T tau, int* __restrict__ npert) {
+__global__ void k_panel_diag(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
+                             T* __restrict__ front, T* __restrict__ dinv, int* __restrict__ piv, T tau,
+                             int* __restrict__ npert) {
     const FrontDev fr = fronts[lf[blockIdx.x]];
     if (fr.nf <= p) return;
-    const int bb = min(B, fr.nf - p), F = fr.F, nf = fr.nf, tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
+    const int bb = min(B, fr.nf - p), F = fr.F, tid = threadIdx.x;
     T* A = front + fr.off;
-    __shared__ T wv[NTP / 32];
-    __shared__ int wr[NTP / 32];
-    __shared__ int prow;
     __shared__ T S[B][B + 1];
     __shared__ T X[B][B + 1];
-    for (int jj = 0; jj < bb; ++jj) {
-        const int j = p + jj;
-        T* colj = A + int64_t(j) * F;
-        // pivot search over rows [j, nf)
-        T bv = T(-1);
-        int br = j;
-        for (int r = j + tid; r < nf; r += NTP) {
-            T v = abs(colj[r]);
-            if (v > bv) { bv = v; br = r; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            T ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            int orr = __shfl_xor_sync(0xffffffffu, br, o);
-            if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
-        }
-        if (lane == 0) { wv[warp] = bv; wr[warp] = br; }
-        __syncthreads();
-        if (tid == 0) {
-            T b0 = wv[0];
-            int r0 = wr[0];
-            for (int q = 1; q < NTP / 32; ++q)
-                if (wv[q] > b0 || (wv[q] == b0 && wr[q] < r0)) { b0 = wv[q]; r0 = wr[q]; }
-            prow = r0;
-            piv[fr.red0 + j] = r0;
+    __shared__ int perm[B];
+    __shared__ int prow;
+    for (int e = tid; e < bb * bb; e += blockDim.x) {
+        int r = e % bb, c = e / bb;
+        S[r][c] = A[int64_t(p + c) * F + p + r];
+    }
+    if (tid < bb) perm[tid] = tid;
+    __syncthreads();
+    for (int j = 0; j < bb; ++j) {
+        if (tid < 32) {
+            T bv = T(-1);
+            int br = j;
+            for (int r = j + tid; r < bb; r += 32) {
+                T v = abs(S[r][j]);
+                if (v > bv) { bv = v; br = r; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                int orr = __shfl_xor_sync(0xffffffffu, br, o);
+                if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
+            }
+            if (tid == 0) prow = br;
         }
         __syncthreads();
         const int pr = prow;
-        if (pr != j)   // swap whole panel rows
-            for (int c = tid; c < bb; c += NTP) {
-                T* col = A + int64_t(p + c) * F;
-                T t = col[j];
-                col[j] = col[pr];
-                col[pr] = t;
+        if (pr != j) {
+            for (int c = tid; c < bb; c += blockDim.x) {
+                T t = S[j][c];
+                S[j][c] = S[pr][c];
+                S[pr][c] = t;
             }
+            if (tid == 0) {
+                int t = perm[j];
+                perm[j] = perm[pr];
+                perm[pr] = t;
+            }
+        }
         __syncthreads();
         if (tid == 0) {
-            T d = colj[j];
             T scale = T(0);
-            for (int c = 0; c < bb; ++c) scale = max(scale, abs(A[int64_t(p + c) * F + j]));
-            if (!(abs(d) > tau * scale)) {
-                colj[j] = (d < T(0) ? -tau : tau) * (scale > T(0) ? scale : T(1));
+            for (int c = j; c < bb; ++c) scale = max(scale, abs(S[j][c]));
+            if (!(abs(S[j][j]) > tau * scale)) {
+                S[j][j] = (S[j][j] < T(0) ? -tau : tau) * (scale > T(0) ? scale : T(1));
                 atomicAdd(npert, 1);
             }
         }
         __syncthreads();
-        const T dinvv = T(1) / colj[j];
-        for (int r = j + 1 + tid; r < F; r += NTP) colj[r] *= dinvv;
+        const T d = S[j][j];
+        for (int r = j + 1 + tid; r < bb; r += blockDim.x) S[r][j] /= d;
         __syncthreads();
-        // rank-1 update of the remaining panel columns
-        const int wcols = bb - jj - 1;
-        if (wcols > 0) {
-            const int64_t tot = int64_t(F - j - 1) * wcols;
-            for (int64_t e = tid; e < tot; e += NTP) {
-                int r = j + 1 + int(e % (F - j - 1));
-                int c = p + jj + 1 + int(e / (F - j - 1));
-                A[int64_t(c) * F + r] -= colj[r] * A[int64_t(c) * F + j];
-            }
+        const int w = bb - j - 1;
+        for (int e = tid; e < w * w; e += blockDim.x) {
+            int r = j + 1 + e % w, c = j + 1 + e / w;
+            S[r][c] -= S[r][j] * S[j][c];
         }
         __syncthreads();
     }
-    for (int e = tid; e < bb * bb; e += NTP) S[e % bb][e / bb] = A[int64_t(p + e / bb) * F + p + e % bb];
-    __syncthreads();
+    for (int e = tid; e < bb * bb; e += blockDim.x) {
+        int r = e % bb, c = e / bb;
+        A[int64_t(p + c) * F + p + r] = S[r][c];
+    }
+    if (tid < bb) piv[fr.red0 + p + tid] = perm[tid];
     if (tid < bb) {   // inverse of the unit-lower factor
         const int c = tid;
         for (int r = 0; r < bb; ++r) X[r][c] = T(0);
@@ -515,7 +511,7 @@ __global__ void __launch_bounds__(NTP) k_panel(const FrontDev* __restrict__ fron
     }
     __syncthreads();
     T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
-    for (int e = tid; e < B * B; e += NTP) Di[e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
+    for (int e = tid; e < B * B; e += blockDim.x) Di[e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
     __syncthreads();
     if (tid < bb) {   // inverse of the upper factor
         const int c = tid;
@@ -528,44 +524,72 @@ __global__ void __launch_bounds__(NTP) k_panel(const FrontDev* __restrict__ fron
         }
     }
     __syncthreads();
-    for (int e = tid; e < B * B; e += NTP) Di[B * B + e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
+    for (int e = tid; e < B * B; e += blockDim.x) Di[B * B + e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
 }
 
-// the row interchanges of panel p applied (in order) to the columns right of
-// the panel, then U12 = Linv * A(p:p+bb, c)
+// The block row permutation of panel p applied to every column outside the
+// diagonal block (left columns: row order of L becomes final; right columns:
+// followed by U12 = Linv * A(p:p+bb, c)).
 template <class T, int B>
-__global__ void k_u12(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p, T* __restrict__ front,
-                      const T* __restrict__ dinv, const int* __restrict__ piv) {
+__global__ void k_rowperm_u12(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
+                              T* __restrict__ front, const T* __restrict__ dinv, const int* __restrict__ piv) {
     const FrontDev fr = fronts[lf[blockIdx.y]];
     if (fr.nf <= p) return;
     const int bb = min(B, fr.nf - p), F = fr.F;
     __shared__ T Li[B][B];
-    __shared__ int pv[B];
+    __shared__ int perm[B];
     const T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
     for (int e = threadIdx.x; e < B * B; e += blockDim.x) Li[e / B][e % B] = Di[e];
-    if (threadIdx.x < bb) pv[threadIdx.x] = piv[fr.red0 + p + threadIdx.x];
+    if (threadIdx.x < bb) perm[threadIdx.x] = piv[fr.red0 + p + threadIdx.x];
     __syncthreads();
-    const int c = p + bb + blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;   // skip the diagonal block
+    if (c >= p) c += bb;
     if (c >= F) return;
-    T* col = front + fr.off + int64_t(c) * F;
-    for (int jj = 0; jj < bb; ++jj) {
-        int pr = pv[jj];
-        if (pr != p + jj) {
-            T t = col[p + jj];
-            col[p + jj] = col[pr];
-            col[pr] = t;
-        }
-    }
+    T* col = front + fr.off + int64_t(c) * F + p;
     T v[B];
 #pragma unroll
-    for (int r = 0; r < B; ++r) v[r] = r < bb ? col[p + r] : T(0);
+    for (int r = 0; r < B; ++r) v[r] = r < bb ? col[perm[r]] : T(0);
+    if (c < p) {
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+            if (r < bb) col[r] = v[r];
+        return;
+    }
 #pragma unroll
     for (int r = B - 1; r >= 0; --r) {
         if (r < bb) {
             T s = v[r];
 #pragma unroll
             for (int q = 0; q < r; ++q) s += Li[r][q] * v[q];
-            col[p + r] = s;
+            col[r] = s;
+        }
+    }
+}
+
+// L21 = A(p+bb:F, p:p+bb) * Uinv
+template <class T, int B>
+__global__ void k_l21(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p, T* __restrict__ front,
+                      const T* __restrict__ dinv) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    if (fr.nf <= p) return;
+    const int bb = min(B, fr.nf - p), F = fr.F;
+    __shared__ T Ui[B][B];
+    const T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B + B * B;
+    for (int e = threadIdx.x; e < B * B; e += blockDim.x) Ui[e / B][e % B] = Di[e];
+    __syncthreads();
+    const int r = p + bb + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= F) return;
+    T* A = front + fr.off;
+    T v[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) v[c] = c < bb ? A[int64_t(p + c) * F + r] : T(0);
+#pragma unroll
+    for (int c = 0; c < B; ++c) {
+        if (c < bb) {
+            T s = T(0);
+#pragma unroll
+            for (int q = 0; q <= c; ++q) s += v[q] * Ui[q][c];
+            A[int64_t(p + c) * F + r] = s;
         }
     }
 }
@@ -625,6 +649,197 @@ __global__ void __launch_bounds__(256) k_gemm(const FrontDev* __restrict__ front
 }
 
 // ---------------------------------------------------------------------------
+// explicit inverses for the solve phase: after its LU, every front holds
+//   Linv11 (strict lower part, unit diagonal), Uinv11 (upper part),
+//   G = L21 * Linv11 in place of L21 and H = Uinv11 * U12 in place of U12,
+// so forward and backward substitution become one GEMV per level.
+// ---------------------------------------------------------------------------
+enum { MD_DENSE = 0, MD_LOWER_UNIT = 1, MD_UPPER = 2 };
+template <class T, int MODE>
+__device__ __forceinline__ T opld(const T* A, int F, int r, int c) {
+    if (MODE == MD_DENSE) return A[int64_t(c) * F + r];
+    if (MODE == MD_LOWER_UNIT) return r > c ? A[int64_t(c) * F + r] : (r == c ? T(1) : T(0));
+    return r <= c ? A[int64_t(c) * F + r] : T(0);
+}
+
+// write the inverted diagonal blocks (Linv_jj strict lower, Uinv_jj upper)
+template <class T, int B>
+__global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ front,
+                               const T* __restrict__ dinv) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int nblk = (fr.nf + B - 1) / B;
+    if (int(blockIdx.x) >= nblk) return;
+    const int p = blockIdx.x * B, bb = min(B, fr.nf - p);
+    const T* Di = dinv + fr.dinv_off + int64_t(blockIdx.x) * 2 * B * B;
+    T* A = front + fr.off;
+    for (int e = threadIdx.x; e < bb * bb; e += blockDim.x) {
+        int r = e / bb, c = e % bb;
+        A[int64_t(p + c) * fr.F + p + r] = r > c ? Di[r * B + c] : Di[B * B + r * B + c];
+    }
+}
+
+// One block-row step of the blocked triangular inversions, into scratch:
+//   LOWER (step i >= 1):  X[Ri, 0:iB]  = -Linv_ii * (L[Ri, 0:iB] * X[0:iB, 0:iB])
+//   UPPER (step i):       Y[Ri, iB+bb:nf] = -Uinv_ii * (U[Ri, iB+bb:nf] * Y[iB+bb:nf, iB+bb:nf])
+// One CTA per (front, 64-column tile); bb <= B <= 32 rows.
+template <class T, int B, bool UPPER>
+__global__ void __launch_bounds__(256) k_trinv_step(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                                    int i, T* __restrict__ front, const T* __restrict__ dinv,
+                                                    T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int nblk = (fr.nf + B - 1) / B;
+    if (i >= nblk || (!UPPER && i == 0)) return;
+    const int r0 = i * B, bb = min(B, fr.nf - r0), F = fr.F;
+    const int cbeg = UPPER ? r0 + bb : 0, cend = UPPER ? fr.nf : r0;
+    const int c0 = cbeg + blockIdx.x * 64;
+    if (c0 >= cend) return;
+    const T* A = front + fr.off;
+    __shared__ T As[B][33];     // A[r0 + rr, k0 + kk]
+    __shared__ T Xs[32][65];    // X[k0 + kk, c0 + cc]
+    __shared__ T Ts[B][65];
+    const int tid = threadIdx.x, cc = tid % 64, rq = tid / 64;   // 4 row groups
+    T acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = T(0);
+    // k range: LOWER: [c0, r0) (X lower: k >= c); UPPER: [cbeg, min(cend, c0 + 64))
+    const int kb = UPPER ? cbeg : c0, ke = UPPER ? min(cend, c0 + 64) : r0;
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+        for (int e = tid; e < B * 32; e += 256) {
+            int rr = e % B, kk = e / B;
+            As[rr][kk] = (rr < bb && k0 + kk < ke) ? A[int64_t(k0 + kk) * F + r0 + rr] : T(0);
+        }
+        for (int e = tid; e < 32 * 64; e += 256) {
+            int kk = e % 32, c = e / 32;
+            int gk = k0 + kk, gc = c0 + c;
+            T v = T(0);
+            if (gk < ke && gc < cend)
+                v = UPPER ? opld<T, MD_UPPER>(A, F, gk, gc) : opld<T, MD_LOWER_UNIT>(A, F, gk, gc);
+            Xs[kk][c] = v;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; ++kk) {
+            T xv = Xs[kk][cc];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] += As[rq * 8 + q][kk] * xv;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Ts[rq * 8 + q][cc] = acc[q];
+    __syncthreads();
+    const T* Di = dinv + fr.dinv_off + int64_t(i) * 2 * B * B + (UPPER ? B * B : 0);
+    T* S = scratch + sc_off[blockIdx.y];
+    if (c0 + cc < cend) {
+        for (int q = 0; q < 8; ++q) {
+            int r = rq * 8 + q;
+            if (r >= bb) continue;
+            T sum = T(0);
+            for (int t = 0; t < bb; ++t) sum += Di[r * B + t] * Ts[t][cc];
+            S[int64_t(c0 + cc - cbeg) * B + r] = -sum;
+        }
+    }
+}
+template <class T, int B, bool UPPER>
+__global__ void k_trinv_copy(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int i,
+                             T* __restrict__ front, const T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int nblk = (fr.nf + B - 1) / B;
+    if (i >= nblk || (!UPPER && i == 0)) return;
+    const int r0 = i * B, bb = min(B, fr.nf - r0);
+    const int cbeg = UPPER ? r0 + bb : 0, cend = UPPER ? fr.nf : r0;
+    const int64_t tot = int64_t(cend - cbeg) * bb;
+    const T* S = scratch + sc_off[blockIdx.y];
+    T* A = front + fr.off;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+        int r = int(e % bb), c = int(e / bb);
+        A[int64_t(cbeg + c) * fr.F + r0 + r] = S[int64_t(c) * B + r];
+    }
+}
+
+// G = L21 * Linv11 (rows nf:F) or H = Uinv11 * U12 (columns nf:F), 64x64 tiles into scratch
+template <class T, bool HMAT>
+__global__ void __launch_bounds__(256) k_gh(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                            const T* __restrict__ front, T* __restrict__ scratch,
+                                            const int64_t* __restrict__ sc_off) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int nf = fr.nf, nb = fr.nb, F = fr.F;
+    if (nf == 0 || nb == 0) return;
+    const int M = HMAT ? nf : nb, N = HMAT ? nb : nf;
+    const int tm = (M + 63) / 64, tn = (N + 63) / 64;
+    if (int(blockIdx.x) >= tm * tn) return;
+    const int i0 = (blockIdx.x % tm) * 64, j0 = (blockIdx.x / tm) * 64;
+    const T* A = front + fr.off;
+    __shared__ T As[32][65];
+    __shared__ T Bs[32][65];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+    // G(r, c) = sum_k L21(r, k) X(k, c), k in [c, nf): k from j0
+    // H(r, c) = sum_k Y(r, k) U12(k, c), k in [r, nf): k from i0
+    const int kb = HMAT ? i0 : j0;
+    for (int k0 = kb; k0 < nf; k0 += 32) {
+        for (int e = tid; e < 32 * 64; e += 256) {
+            int ii = e % 64, kk = e / 64;
+            int r = i0 + ii, k = k0 + kk;
+            T v = T(0);
+            if (r < M && k < nf) v = HMAT ? opld<T, MD_UPPER>(A, F, r, k) : A[int64_t(k) * F + nf + r];
+            As[kk][ii] = v;
+        }
+        for (int e = tid; e < 32 * 64; e += 256) {
+            int kk = e % 32, jj = e / 32;
+            int k = k0 + kk, c = j0 + jj;
+            T v = T(0);
+            if (c < N && k < nf) v = HMAT ? A[int64_t(nf + c) * F + k] : opld<T, MD_LOWER_UNIT>(A, F, k, c);
+            Bs[kk][jj] = v;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; ++kk) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[kk][tx * 4 + a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][ty * 4 + b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+        }
+        __syncthreads();
+    }
+    T* S = scratch + sc_off[blockIdx.y];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        int c = j0 + ty * 4 + b;
+        if (c >= N) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            int r = i0 + tx * 4 + a;
+            if (r < M) S[int64_t(c) * M + r] = acc[a][b];
+        }
+    }
+}
+template <class T, bool HMAT>
+__global__ void k_gh_copy(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ front,
+                          const T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int nf = fr.nf, nb = fr.nb;
+    const int M = HMAT ? nf : nb;
+    const int64_t tot = int64_t(nf) * nb;
+    const T* S = scratch + sc_off[blockIdx.y];
+    T* A = front + fr.off;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+        int r = int(e % M), c = int(e / M);
+        if (HMAT) A[int64_t(nf + c) * fr.F + r] = S[e];
+        else A[int64_t(c) * fr.F + nf + r] = S[e];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // solve phase
 // ---------------------------------------------------------------------------
 // reduced, row-scaled rhs: wet rows minus the couplings to the eliminated
@@ -640,27 +855,39 @@ __global__ void k_reduce_rhs(int nred, const int* __restrict__ r2g, const char* 
         double s = double(r[g]);
         for (int e = rp[g]; e < rp[g + 1]; ++e) {
             int c = ci[e];
-            if (isdry[c]) s -= val[e] * double(r[c]);
+            if (isdry[c] == 1) s -= val[e] * double(r[c]);
         }
         red[q] = dr[g] * s;
     }
 }
+// Identity rows (isdry 1) pass r through; pinned pressures (isdry 2) are the
+// gauge of J's null space and come out as exact zeros, so every solution the
+// solver returns has zero pressure at the pins.
 template <class TV>
-__global__ void k_expand(int ndim, const int* __restrict__ g2r, const double* __restrict__ dc,
-                         const double* __restrict__ red, const TV* __restrict__ r, TV* __restrict__ z) {
+__global__ void k_expand(int ndim, const int* __restrict__ g2r, const char* __restrict__ isdry,
+                         const double* __restrict__ dc, const double* __restrict__ red, const TV* __restrict__ r,
+                         TV* __restrict__ z) {
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ndim; g += gridDim.x * blockDim.x) {
         int q = g2r[g];
-        z[g] = q >= 0 ? TV(dc[g] * red[q]) : r[g];
+        z[g] = q >= 0 ? TV(dc[g] * red[q]) : (isdry[g] == 2 ? TV(0) : r[g]);
     }
 }
 
-// forward elimination of one level: one CTA per front
-template <class T, int B>
-__global__ void __launch_bounds__(NT) k_fwd(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                            const int* __restrict__ child_of, const int* __restrict__ emap,
-                                            const T* __restrict__ front, const T* __restrict__ dinv,
-                                            const int* __restrict__ piv, const double* __restrict__ red,
-                                            double* __restrict__ W) {
+// Solve phase, one level at a time (all fronts of the level together).
+// Work items split every front into (256-row tile, 256-column chunk) pieces
+// so the GEMVs spread over all SMs; partial sums per chunk are reduced in a
+// second pass (deterministic order). Accumulation is FP64.
+struct WorkItem {
+    int front, row0, col0, chunk;
+};
+constexpr int GR = 256, GC = 256;
+
+// forward prologue: w = [red_C ; 0] + children's update vectors, then the
+// block-local row permutations applied to the own part (into wp)
+__global__ void __launch_bounds__(NT) k_fwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                                   const int* __restrict__ child_of, const int* __restrict__ emap,
+                                                   const int* __restrict__ piv, const double* __restrict__ red,
+                                                   double* __restrict__ W, double* __restrict__ WP, int B) {
     const int f = lf[blockIdx.x];
     const FrontDev fr = fronts[f];
     const int F = fr.F, nf = fr.nf, tid = threadIdx.x;
@@ -671,84 +898,90 @@ __global__ void __launch_bounds__(NT) k_fwd(const FrontDev* __restrict__ fronts,
         int c = child_of[2 * f + s];
         if (c < 0) continue;
         const FrontDev ch = fronts[c];
-        const double* u = W + ch.woff + ch.nf;
+        const double* u = WP + ch.woff + ch.nf;   // child's update vector
         const int* em = emap + ch.emap_off;
         for (int a = tid; a < ch.nb; a += NT) w[em[a]] += u[a];
         __syncthreads();
     }
-    const T* A = front + fr.off;
-    __shared__ double t[B], y[B];
-    for (int p = 0; p < nf; p += B) {
-        const int bb = min(B, nf - p);
-        if (tid == 0)
-            for (int jj = 0; jj < bb; ++jj) {
-                int pr = piv[fr.red0 + p + jj];
-                if (pr != p + jj) {
-                    double tmp = w[p + jj];
-                    w[p + jj] = w[pr];
-                    w[pr] = tmp;
-                }
-            }
-        __syncthreads();
-        if (tid < bb) t[tid] = w[p + tid];
-        __syncthreads();
-        const T* Li = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
-        if (tid < bb) {
-            double s = t[tid];
-            for (int q = 0; q < tid; ++q) s += double(Li[tid * B + q]) * t[q];
-            y[tid] = s;
-            w[p + tid] = s;
+    double* wp = WP + fr.woff;
+    for (int q = tid; q < F; q += NT) {
+        if (q < nf) {
+            int p = (q / B) * B;
+            wp[q] = w[p + piv[fr.red0 + q]];
+        } else {
+            wp[q] = w[q];
         }
-        __syncthreads();
-        for (int r = p + bb + tid; r < F; r += NT) {
-            double s = w[r];
-            for (int c = 0; c < bb; ++c) s -= double(A[int64_t(p + c) * F + r]) * y[c];
-            w[r] = s;
-        }
-        __syncthreads();
     }
 }
-
-// backward substitution of one level: one CTA per front; warp lanes map to
-// the rows of a panel, warps split the columns.
-template <class T, int B>
-__global__ void __launch_bounds__(NT) k_bwd(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                            const int* __restrict__ vars, const T* __restrict__ front,
-                                            const T* __restrict__ dinv, double* __restrict__ W,
-                                            double* __restrict__ xred) {
-    static_assert(B <= 32, "panel must fit a warp");
-    const FrontDev fr = fronts[lf[blockIdx.x]];
-    const int F = fr.F, nf = fr.nf, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double* w = W + fr.woff;
-    const int* vv = vars + fr.voff;
-    for (int q = nf + tid; q < F; q += NT) w[q] = xred[vv[q]];
+// partial GEMV products: forward rows [0,F) x own columns; backward own rows x [0,F)
+template <class T, bool BWD>
+__global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
+                                                  const T* __restrict__ front, const double* __restrict__ X,
+                                                  double* __restrict__ part, const int64_t* __restrict__ part_off) {
+    const WorkItem it = items[blockIdx.x];
+    const FrontDev fr = fronts[it.front];
+    const int F = fr.F, nf = fr.nf;
+    const int r = it.row0 + threadIdx.x;
+    const int nrows = BWD ? nf : F, ncols = BWD ? F : nf;
+    __shared__ double xs[GC];
+    const double* x = X + fr.woff;
+    for (int q = threadIdx.x; q < GC; q += GR) xs[q] = it.col0 + q < ncols ? x[it.col0 + q] : 0.0;
     __syncthreads();
+    if (r >= nrows) return;
     const T* A = front + fr.off;
-    __shared__ double part[NT / 32][B];
-    __shared__ double t[B];
-    const int npan = (nf + B - 1) / B;
-    for (int pi = npan - 1; pi >= 0; --pi) {
-        const int p = pi * B, bb = min(B, nf - p);
-        double s = 0.0;
-        if (lane < bb)
-            for (int c = p + bb + warp; c < F; c += NT / 32) s += double(A[int64_t(c) * F + p + lane]) * w[c];
-        part[warp][lane] = s;
-        __syncthreads();
-        if (tid < bb) {
-            double acc = w[p + tid];
-            for (int q = 0; q < NT / 32; ++q) acc -= part[q][tid];
-            t[tid] = acc;
+    double s = 0.0;
+    const int cend = min(ncols, it.col0 + GC);
+    if (!BWD) {
+        // rows < nf: Linv11 (lower, unit diagonal); rows >= nf: -G
+        if (r < nf) {
+            const int ce = min(cend, r);
+            for (int c = it.col0; c < ce; ++c) s += double(A[int64_t(c) * F + r]) * xs[c - it.col0];
+            if (r >= it.col0 && r < cend) s += xs[r - it.col0];
+        } else {
+            for (int c = it.col0; c < cend; ++c) s -= double(A[int64_t(c) * F + r]) * xs[c - it.col0];
         }
-        __syncthreads();
-        const T* Ui = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B + B * B;
-        if (tid < bb) {
-            double x = 0.0;
-            for (int q = tid; q < bb; ++q) x += double(Ui[tid * B + q]) * t[q];
-            w[p + tid] = x;
+    } else {
+        // columns < nf: Uinv11 (upper incl. diagonal); columns >= nf: -H
+        for (int c = max(it.col0, r); c < cend; ++c) {
+            double a = double(A[int64_t(c) * F + r]);
+            s += c < nf ? a * xs[c - it.col0] : -a * xs[c - it.col0];
         }
-        __syncthreads();
     }
-    for (int q = tid; q < nf; q += NT) xred[fr.red0 + q] = w[q];
+    part[part_off[it.front] + int64_t(it.chunk) * F + r] = s;
+}
+// forward epilogue: own rows -> y (kept in W), boundary rows -> update vector in WP
+__global__ void k_fwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                             const double* __restrict__ part, const int64_t* __restrict__ part_off,
+                             double* __restrict__ W, double* __restrict__ WP) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fr.F) return;
+    const int nch = (fr.nf + GC - 1) / GC;
+    double s = 0.0;
+    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.F + r];
+    if (r < fr.nf) W[fr.woff + r] = s;                     // y
+    else WP[fr.woff + r] = WP[fr.woff + r] + s;            // u = w_B - G w_C
+}
+// backward prologue: X = [y ; x_B]
+__global__ void k_bwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, const int* __restrict__ vars,
+                             const double* __restrict__ W, const double* __restrict__ xred, double* __restrict__ WP) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.F) return;
+    WP[fr.woff + q] = q < fr.nf ? W[fr.woff + q] : xred[vars[fr.voff + q]];
+}
+__global__ void k_bwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                             const double* __restrict__ part, const int64_t* __restrict__ part_off,
+                             double* __restrict__ xred) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fr.nf) return;
+    const int nch = (fr.F + GC - 1) / GC;
+    double s = 0.0;
+    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.F + r];
+    xred[fr.red0 + r] = s;
 }
 
 __global__ void k_fill(int n, double v, double* __restrict__ a) {
@@ -820,6 +1053,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_g2r = upload(lu, plan.g2r, s);
     std::vector<char> isdry(plan.ndim, 0);
     for (int r : plan.dry_rows) isdry[r] = 1;
+    for (int r : plan.pins) isdry[r] = 2;
     lu.d_isdry = upload(lu, isdry, s);
     lu.d_asm_src = upload(lu, plan.asm_src, s);
     lu.d_asm_dst = upload(lu, plan.asm_dst, s);
@@ -834,6 +1068,58 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_dc = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_cmax = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_npert = static_cast<int*>(dmalloc(lu, sizeof(int)));
+    lu.d_wp = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
+    // solve-phase work items and partial-sum offsets
+    std::vector<WorkItem> fi, bi;
+    std::vector<int64_t> part_off(plan.nfronts, 0);
+    int64_t poff = 0;
+    for (int f = 0; f < plan.nfronts; ++f) {
+        const FrontDev& fr = plan.fronts[f];
+        part_off[f] = poff;
+        poff += int64_t(fr.F) * ((fr.F + GC - 1) / GC);
+    }
+    lu.fwd_items_start.clear();
+    lu.bwd_items_start.clear();
+    lu.fwd_bytes.assign(plan.nlevels, 0.0);
+    lu.bwd_bytes.assign(plan.nlevels, 0.0);
+    for (int h = 0; h < plan.nlevels; ++h) {
+        lu.fwd_items_start.push_back(int(fi.size()));
+        lu.bwd_items_start.push_back(int(bi.size()));
+        for (int f : plan.level_fronts[h]) {
+            const FrontDev& fr = plan.fronts[f];
+            const double nf = fr.nf, nb = fr.nb;
+            // forward: strict lower Linv11 + G (nb x nf); backward: upper Uinv11 + H (nf x nb)
+            lu.fwd_bytes[h] += double(ts) * (nf * (nf - 1) / 2 + nb * nf);
+            lu.bwd_bytes[h] += double(ts) * (nf * (nf + 1) / 2 + nf * nb);
+            for (int c = 0; c * GC < fr.nf; ++c)
+                for (int r = 0; r * GR < fr.F; ++r) fi.push_back(WorkItem{f, r * GR, c * GC, c});
+            for (int c = 0; c * GC < fr.F; ++c)
+                for (int r = 0; r * GR < fr.nf; ++r) bi.push_back(WorkItem{f, r * GR, c * GC, c});
+        }
+    }
+    lu.fwd_items_start.push_back(int(fi.size()));
+    lu.bwd_items_start.push_back(int(bi.size()));
+    lu.d_fwd_items = upload(lu, fi, s);
+    lu.d_bwd_items = upload(lu, bi, s);
+    lu.d_part_off = upload(lu, part_off, s);
+    lu.d_part = dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(poff, 1)));
+    // factorisation scratch (per level, per front)
+    std::vector<int64_t> sct, scg;
+    int64_t mx = 0;
+    for (int h = 0; h < plan.nlevels; ++h) {
+        int64_t a = 0, b = 0;
+        for (int f : plan.level_fronts[h]) {
+            const FrontDev& fr = plan.fronts[f];
+            sct.push_back(a);
+            a += int64_t(plan.panel) * fr.nf;
+            scg.push_back(b);
+            b += int64_t(fr.nf) * fr.nb;
+        }
+        mx = std::max(mx, std::max(a, b));
+    }
+    lu.d_sc_tr = upload(lu, sct, s);
+    lu.d_sc_gh = upload(lu, scg, s);
+    lu.d_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(mx, 1)));
     ck(cudaStreamSynchronize(s));
 }
 
@@ -841,13 +1127,13 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
 static void equilibrate(NdLu& lu, const int* rp, const int* ci, const double* val, cudaStream_t s) {
     const NdPlan& P = *lu.plan;
     const int nd = P.ndim, G = blocks_for(nd);
-    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dr);
-    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dc);
+    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dr); IEMIC_COUNT_LAUNCH();
+    k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dc); IEMIC_COUNT_LAUNCH();
     for (int it = 0; it < 3; ++it) {
-        k_rowmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dc, lu.d_dr);
+        k_rowmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dc, lu.d_dr); IEMIC_COUNT_LAUNCH();
         ck(cudaMemsetAsync(lu.d_cmax, 0, sizeof(double) * nd, s));
-        k_colmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dr, lu.d_dc, lu.d_cmax);
-        k_colscale<<<G, NT, 0, s>>>(nd, lu.d_g2r, lu.d_cmax, lu.d_dc);
+        k_colmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dr, lu.d_dc, lu.d_cmax); IEMIC_COUNT_LAUNCH();
+        k_colscale<<<G, NT, 0, s>>>(nd, lu.d_g2r, lu.d_cmax, lu.d_dc); IEMIC_COUNT_LAUNCH();
     }
 }
 
@@ -856,13 +1142,14 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
     const NdPlan& P = *lu.plan;
     T* front = static_cast<T*>(lu.d_front);
     T* dinv = static_cast<T*>(lu.d_dinv);
+    T* scratch = static_cast<T*>(lu.d_scratch);
     const T tau = sizeof(T) == 4 ? T(1e-7) : T(1e-15);
     equilibrate(lu, rp, ci, values, s);
     ck(cudaMemsetAsync(front, 0, sizeof(T) * size_t(P.front_entries), s));
     ck(cudaMemsetAsync(lu.d_npert, 0, sizeof(int), s));
     const int64_t na = int64_t(P.asm_src.size());
     k_assemble<T><<<blocks_for(na), NT, 0, s>>>(na, lu.d_asm_src, lu.d_asm_dst, lu.d_asm_row, ci, values, lu.d_dr,
-                                                lu.d_dc, front);
+                                                lu.d_dc, front); IEMIC_COUNT_LAUNCH();
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
@@ -873,17 +1160,57 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
             for (int c : P.level_children[sl][h]) mx = std::max<int64_t>(mx, int64_t(P.fronts[c].nb) * P.fronts[c].nb);
             dim3 g(blocks_for(mx), nc);
             k_extend_add<T><<<g, NT, 0, s>>>(lu.d_fronts, lu.d_level_children[sl] + lu.child_start[sl][h], lu.d_emap,
-                                             front);
+                                             front); IEMIC_COUNT_LAUNCH();
         }
         const int maxnf = P.level_maxnf[h], maxF = P.level_maxF[h];
         for (int p = 0; p < maxnf; p += B) {
-            k_panel<T, B><<<nfr, NTP, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert);
-            const int rest = maxF - p;
-            dim3 g1((rest + NT - 1) / NT, nfr);
-            k_u12<T, B><<<g1, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv);
-            const int tiles = (rest + 63) / 64;
+            k_panel_diag<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert); IEMIC_COUNT_LAUNCH();
+            dim3 g1((maxF + NT - 1) / NT, nfr);
+            k_rowperm_u12<T, B><<<g1, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv); IEMIC_COUNT_LAUNCH();
+            dim3 g3((maxF - p + NT - 1) / NT, nfr);
+            k_l21<T, B><<<g3, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv); IEMIC_COUNT_LAUNCH();
+            const int tiles = (maxF - p + 63) / 64;
             dim3 g2(tiles * tiles, nfr);
-            k_gemm<T, B><<<g2, 256, 0, s>>>(lu.d_fronts, lf, p, front);
+            cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
+            k_gemm<T, B><<<g2, 256, 0, s>>>(lu.d_fronts, lf, p, front); IEMIC_COUNT_LAUNCH();
+            if (ev) {
+                double fl = 0.0, by = 0.0;   // 2 M^2 bb flops; A read+write, panels read once
+                for (int f : P.level_fronts[h]) {
+                    const FrontDev& fr = P.fronts[f];
+                    if (fr.nf <= p) continue;
+                    const double bb = std::min(B, fr.nf - p), M = fr.F - p - bb;
+                    fl += 2.0 * M * M * bb;
+                    by += double(sizeof(T)) * (2.0 * M * M + 2.0 * M * bb);
+                }
+                lu.timer->stop(ev, s, IEMIC_KC_FACTOR_GEMM, by, fl);
+            }
+        }
+        // explicit inverses for the solve phase
+        const int maxblk = (maxnf + B - 1) / B;
+        const int64_t* sct = lu.d_sc_tr + lu.level_start[h];
+        const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
+        k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
+        const int ctiles = (maxnf + 63) / 64;
+        const int cblocks = blocks_for(int64_t(maxnf) * B);
+        for (int i = 1; i < maxblk; ++i) {
+            k_trinv_step<T, B, false><<<dim3(ctiles, nfr), 256, 0, s>>>(lu.d_fronts, lf, i, front, dinv, scratch, sct); IEMIC_COUNT_LAUNCH();
+            k_trinv_copy<T, B, false><<<dim3(cblocks, nfr), NT, 0, s>>>(lu.d_fronts, lf, i, front, scratch, sct); IEMIC_COUNT_LAUNCH();
+        }
+        for (int i = maxblk - 2; i >= 0; --i) {
+            k_trinv_step<T, B, true><<<dim3(ctiles, nfr), 256, 0, s>>>(lu.d_fronts, lf, i, front, dinv, scratch, sct); IEMIC_COUNT_LAUNCH();
+            k_trinv_copy<T, B, true><<<dim3(cblocks, nfr), NT, 0, s>>>(lu.d_fronts, lf, i, front, scratch, sct); IEMIC_COUNT_LAUNCH();
+        }
+        int64_t mt = 0, mnb = 0;
+        for (int f : P.level_fronts[h]) {
+            const FrontDev& fr = P.fronts[f];
+            mt = std::max<int64_t>(mt, int64_t((fr.nf + 63) / 64) * ((fr.nb + 63) / 64));
+            mnb = std::max<int64_t>(mnb, int64_t(fr.nf) * fr.nb);
+        }
+        if (mt > 0) {
+            k_gh<T, false><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+            k_gh_copy<T, false><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+            k_gh<T, true><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+            k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
         }
     }
     ck(cudaGetLastError());
@@ -901,20 +1228,39 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
     const NdPlan& P = *lu.plan;
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
+    double* WP = static_cast<double*>(lu.d_wp);
+    double* part = static_cast<double*>(lu.d_part);
     const T* front = static_cast<const T*>(lu.d_front);
-    const T* dinv = static_cast<const T*>(lu.d_dinv);
-    k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red);
+    k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
-        k_fwd<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lu.d_level_fronts + lu.level_start[h], lu.d_child_of, lu.d_emap,
-                                       front, dinv, lu.d_piv, red, W);
+        const int* lf = lu.d_level_fronts + lu.level_start[h];
+        k_fwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
+        const int ni = lu.fwd_items_start[h + 1] - lu.fwd_items_start[h];
+        cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
+        if (ni) {
+            k_gemv_part<T, false><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_fwd_items) +
+                                                        lu.fwd_items_start[h], front, WP, part, lu.d_part_off); IEMIC_COUNT_LAUNCH();
+        }
+        if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.fwd_bytes[h], 2.0 * lu.fwd_bytes[h] / sizeof(T));
+        k_fwd_reduce<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off, W,
+                                                                                WP); IEMIC_COUNT_LAUNCH();
     }
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
-        k_bwd<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lu.d_level_fronts + lu.level_start[h], lu.d_vars, front, dinv, W,
-                                       red);
+        const int* lf = lu.d_level_fronts + lu.level_start[h];
+        k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
+        const int ni = lu.bwd_items_start[h + 1] - lu.bwd_items_start[h];
+        cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
+        if (ni) {
+            k_gemv_part<T, true><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_bwd_items) +
+                                                       lu.bwd_items_start[h], front, WP, part, lu.d_part_off); IEMIC_COUNT_LAUNCH();
+        }
+        if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.bwd_bytes[h], 2.0 * lu.bwd_bytes[h] / sizeof(T));
+        k_bwd_reduce<<<dim3((P.level_maxnf[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off,
+                                                                                 red); IEMIC_COUNT_LAUNCH();
     }
-    k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_dc, red, r, z);
+    k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dc, red, r, z); IEMIC_COUNT_LAUNCH();
     ck(cudaGetLastError());
 }
 

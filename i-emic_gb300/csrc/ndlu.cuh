@@ -46,9 +46,13 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
                    const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel);
 
 // Device-resident factorisation for one precision.
+struct KTimer;
+
 struct NdLu {
     int prec = 0;   // 0 FP64, 1 FP32
     const NdPlan* plan = nullptr;
+    KTimer* timer = nullptr;                // optional launch timing (owned by the engine)
+    std::vector<double> fwd_bytes, bwd_bytes;   // per level: factor bytes one GEMV sweep reads
     // device copies of the plan
     FrontDev* d_fronts = nullptr;
     int* d_level_fronts = nullptr;          // concatenated per level
@@ -67,6 +71,13 @@ struct NdLu {
     void* d_w = nullptr;                    // solve vectors (T)
     void* d_red = nullptr;                  // reduced rhs / solution (T)
     int* d_npert = nullptr;                 // perturbed-pivot counter
+    void* d_wp = nullptr;                   // permuted / gathered solve vectors (FP64)
+    void* d_part = nullptr;                 // GEMV partial sums (FP64)
+    int64_t* d_part_off = nullptr;
+    void *d_fwd_items = nullptr, *d_bwd_items = nullptr;   // GEMV work items per level
+    std::vector<int> fwd_items_start, bwd_items_start;
+    int64_t *d_sc_tr = nullptr, *d_sc_gh = nullptr;         // scratch offsets per front (by level)
+    void* d_scratch = nullptr;
     int npert = 0;
     bool factored = false;
     std::vector<void*> allocs;

@@ -339,15 +339,22 @@ void Engine::set_par(int idx, double value) {
     jac_valid = false;
 }
 
+// Algorithmic bytes: the state read and the padded fields written and read
+// back (usol), plus the residual (3 vectors) or the CSR values written (FP64
+// and FP32 copies) for the Jacobian.
 void Engine::rhs_dev(const double* x, double* F) {
+    cudaEvent_t ev = timer.start(stream);
     launch_usol(geo, x, d_pads, stream);
     launch_rhs(geo, P, fs, d_al, d_pads, x, d_surf, F, stream);
+    timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 8.0 * 4.0 * ndim, 0.0);
     ck(cudaGetLastError());
 }
 
 void Engine::jacobian_dev(const double* x) {
+    cudaEvent_t ev = timer.start(stream);
     launch_usol(geo, x, d_pads, stream);
     launch_jacobian(geo, P, pat, d_al, d_pads, d_val, d_val32, stream);
+    timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 12.0 * double(nnz) + 8.0 * 3.0 * ndim, 0.0);
     ck(cudaGetLastError());
     jac_valid = true;
     fact64_stale = fact32_stale = true;

@@ -8,6 +8,11 @@
 
 namespace iemic {
 
+// Process-wide count of kernel launches made by this library (read through
+// iemic_launch_count); every launch site is followed by IEMIC_COUNT_LAUNCH().
+long long& launch_counter();
+#define IEMIC_COUNT_LAUNCH() (++::iemic::launch_counter())
+
 // Geometry tables, computed once on the host from the grid exactly as the
 // Fortran atoms compute them (src/ocean/spf.F90), and uploaded. The GPU
 // kernels never call transcendental functions.

@@ -1,6 +1,7 @@
 // C ABI of the linear-solve path (Ocean::solve / applyPrecon /
 // buildPreconditioner, src/ocean/Ocean.C:1070-1147, 1377-1404).
 #include "engine.cuh"
+#include "ndlu.cuh"
 
 using namespace iemic;
 
@@ -12,7 +13,16 @@ using namespace iemic;
     catch (...) { return IEMIC_ERR_CUDA; }                   \
     return IEMIC_OK;
 
+namespace iemic {
+long long& launch_counter() {
+    static long long count = 0;
+    return count;
+}
+}  // namespace iemic
+
 extern "C" {
+
+long long iemic_launch_count(void) { return iemic::launch_counter(); }
 
 void iemic_default_solve_opts(iemic_solve_opts* o) {
     if (!o) return;
@@ -23,6 +33,18 @@ void iemic_default_solve_opts(iemic_solve_opts* o) {
     o->max_refinements = 20;
     o->inner_tol = 1e-4;
     o->transpose = 0;
+    o->reuse_preconditioner = 0;
+}
+
+int iemic_solver_gauge(iemic_ocean* h, int* idx, int capacity, int* count) {
+    if (!h || !count || capacity < 0 || (capacity > 0 && !idx)) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    h->e.ensure_solver();
+    const std::vector<int>& pins = h->e.ndplan->pins;
+    *count = int(pins.size());
+    if (capacity < int(pins.size())) return capacity == 0 ? IEMIC_OK : IEMIC_ERR_ARG;
+    for (size_t q = 0; q < pins.size(); ++q) idx[q] = pins[q];
+    GUARD_END
 }
 
 int iemic_build_preconditioner(iemic_ocean* h, int precision) {
@@ -52,6 +74,7 @@ int iemic_solve_dev(iemic_ocean* h, const double* b, double* x, const iemic_solv
     iemic_default_solve_opts(&oo);
     if (o) oo = *o;
     if (oo.restart < 1 || oo.restart > 1000 || oo.max_iters < 1 || !(oo.tol > 0)) return IEMIC_ERR_ARG;
+    if (oo.precision < 0 || oo.precision > 2) return IEMIC_ERR_ARG;
     iemic_solve_stats s{};
     int rc;
     try {
@@ -82,6 +105,50 @@ int iemic_solve(iemic_ocean* h, const double* b, double* x, const iemic_solve_op
         return IEMIC_ERR_CUDA;
     }
     return rc;
+}
+
+int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out) {
+    if (!h || !out) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    h->e.ensure_solver();
+    const NdPlan& P = *h->e.ndplan;
+    out->unknowns = P.ndim;
+    out->reduced_unknowns = P.nred;
+    out->fronts = P.nfronts;
+    out->levels = P.nlevels;
+    out->factor_entries = P.factor_entries;
+    out->front_entries = P.front_entries;
+    out->factor_flops = P.flops;
+    GUARD_END
+}
+
+int iemic_kernel_timing(iemic_ocean* h, int enable) {
+    if (!h) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    ck(cudaStreamSynchronize(h->e.stream));
+    h->e.timer.drain();
+    if (enable) h->e.timer.reset();
+    h->e.timer.on = enable != 0;
+    GUARD_END
+}
+
+int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out) {
+    if (!h || !out || kclass < 0 || kclass >= IEMIC_KC_COUNT) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    ck(cudaStreamSynchronize(h->e.stream));
+    KTimer& t = h->e.timer;
+    t.drain();
+    out->launches = t.launches[kclass];
+    out->ms = t.ms[kclass];
+    out->bytes = t.bytes[kclass];
+    out->flops = t.flops[kclass];
+    GUARD_END
+}
+
+int iemic_get_stream(iemic_ocean* h, void** stream) {
+    if (!h || !stream) return IEMIC_ERR_ARG;
+    *stream = static_cast<void*>(h->e.stream);
+    return IEMIC_OK;
 }
 
 }  // extern "C"

@@ -706,30 +706,30 @@ int grid_for(size_t work, int block) {
 
 void launch_lin(const Geo& g, const Params& p, double* al_tab, cudaStream_t s) {
     size_t work = size_t(g.m) * g.l * 2 * CELL_ENTRIES;
-    lin_kernel<<<grid_for(work, 256), 256, 0, s>>>(g, p, al_tab);
+    lin_kernel<<<grid_for(work, 256), 256, 0, s>>>(g, p, al_tab); IEMIC_COUNT_LAUNCH();
 }
 void launch_usol(const Geo& g, const double* x, double* pads, cudaStream_t s) {
-    usol_kernel<<<grid_for(g.npad(), 256), 256, 0, s>>>(g, x, pads);
+    usol_kernel<<<grid_for(g.npad(), 256), 256, 0, s>>>(g, x, pads); IEMIC_COUNT_LAUNCH();
 }
 void launch_pattern(const Geo& g, const Pattern& pat, int* col_idx, cudaStream_t s) {
     size_t work = size_t(g.n) * g.m * g.l * CELL_ENTRIES;
-    pattern_kernel<<<grid_for(work, 256), 256, 0, s>>>(g, pat, col_idx);
+    pattern_kernel<<<grid_for(work, 256), 256, 0, s>>>(g, pat, col_idx); IEMIC_COUNT_LAUNCH();
 }
 void launch_jacobian(const Geo& g, const Params& p, const Pattern& pat, const double* al_tab, const double* pads,
                      double* val, float* val32, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
     size_t blocks = (nc + 31) / 32;
-    jacobian_kernel<<<int(blocks), 192, 0, s>>>(g, p, pat, al_tab, pads, val, val32);
+    jacobian_kernel<<<int(blocks), 192, 0, s>>>(g, p, pat, al_tab, pads, val, val32); IEMIC_COUNT_LAUNCH();
 }
 void launch_rhs(const Geo& g, const Params& p, const ForcingScalars& fs, const double* al_tab, const double* pads,
                 const double* x, const double* surf, double* F, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
     size_t blocks = (nc + 31) / 32;
-    rhs_kernel<<<int(blocks), 192, 0, s>>>(g, p, fs, al_tab, pads, x, surf, F);
+    rhs_kernel<<<int(blocks), 192, 0, s>>>(g, p, fs, al_tab, pads, x, surf, F); IEMIC_COUNT_LAUNCH();
 }
 void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
-    mass_kernel<<<grid_for(nc, 256), 256, 0, s>>>(g, p.par[ROSB], diagB);
+    mass_kernel<<<grid_for(nc, 256), 256, 0, s>>>(g, p.par[ROSB], diagB); IEMIC_COUNT_LAUNCH();
 }
 
 }  // namespace iemic

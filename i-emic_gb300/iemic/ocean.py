@@ -28,7 +28,7 @@ PARAMETER_NAMES = {
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "not converged", -4: "NaN/Inf",
           -5: "zero pivot", -6: "call order", -7: "device allocation failed"}
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP32_KRYLOV = 0, 1, 2
 
 
 class IemicError(RuntimeError):
@@ -62,6 +62,61 @@ class SolveStats(ctypes.Structure):
                 ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
 
 
+class NewtonOpts(ctypes.Structure):
+    _fields_ = [("max_iters", ctypes.c_int), ("tol", ctypes.c_double), ("backtracking_steps", ctypes.c_int),
+                ("solve", SolveOpts), ("refactor_each_iter", ctypes.c_int)]
+
+
+class NewtonStats(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int), ("backtracks", ctypes.c_int), ("linear_solves", ctypes.c_int),
+                ("krylov_iters", ctypes.c_int), ("factorizations", ctypes.c_int),
+                ("rhs_norm0", ctypes.c_double), ("rhs_norm", ctypes.c_double),
+                ("time_ms", ctypes.c_double), ("time_assembly_ms", ctypes.c_double),
+                ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
+
+
+class ContinuationOpts(ctypes.Structure):
+    _fields_ = [("par_idx", ctypes.c_int), ("ds", ctypes.c_double), ("ds_min", ctypes.c_double),
+                ("ds_max", ctypes.c_double), ("decrease", ctypes.c_double),
+                ("destination", ctypes.c_double), ("destination_tol", ctypes.c_double),
+                ("max_steps", ctypes.c_int), ("max_newton", ctypes.c_int), ("min_newton", ctypes.c_int),
+                ("opt_newton", ctypes.c_double), ("newton_tol", ctypes.c_double),
+                ("residual_test", ctypes.c_char), ("normalize", ctypes.c_char), ("tangent", ctypes.c_char),
+                ("initial_tangent", ctypes.c_char), ("epsilon", ctypes.c_double),
+                ("tan_scaling", ctypes.c_double), ("predictor_bound", ctypes.c_double),
+                ("backtracking_steps", ctypes.c_int), ("backtracking_increase", ctypes.c_double),
+                ("newton_chord", ctypes.c_int), ("give_up_at_ds_min", ctypes.c_int),
+                ("solve", SolveOpts), ("refactor_each_newton", ctypes.c_int)]
+
+
+class ContinuationStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("failed_steps", ctypes.c_int), ("newton_iters", ctypes.c_int),
+                ("linear_solves", ctypes.c_int), ("unconverged_solves", ctypes.c_int),
+                ("krylov_iters", ctypes.c_int), ("factorizations", ctypes.c_int),
+                ("reached_destination", ctypes.c_int), ("aborted", ctypes.c_int),
+                ("par", ctypes.c_double), ("ds", ctypes.c_double), ("rhs_norm", ctypes.c_double),
+                ("time_ms", ctypes.c_double), ("time_assembly_ms", ctypes.c_double),
+                ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
+
+
+class KernelStats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_longlong), ("ms", ctypes.c_double), ("bytes", ctypes.c_double),
+                ("flops", ctypes.c_double)]
+
+
+class SolverInfo(ctypes.Structure):
+    _fields_ = [("unknowns", ctypes.c_int64), ("reduced_unknowns", ctypes.c_int64), ("fronts", ctypes.c_int64),
+                ("levels", ctypes.c_int64), ("factor_entries", ctypes.c_int64), ("front_entries", ctypes.c_int64),
+                ("factor_flops", ctypes.c_double)]
+
+
+KERNEL_CLASSES = {"factor_gemm": 0, "solve_gemv": 1, "assembly": 2, "spmv": 3}
+
+
+def _asdict(st):
+    return {k: getattr(st, k) for k, _ in st._fields_}
+
+
 # Every entry point of include/iemic_gb300.h with its ctypes signature.
 _VP = ctypes.c_void_p
 _IP = ctypes.POINTER(ctypes.c_int)
@@ -87,7 +142,21 @@ SIGNATURES = {
     "iemic_apply_precon": [_VP, ctypes.c_int, _DP, _DP],
     "iemic_solve": [_VP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats)],
     "iemic_solve_dev": [_VP, _VP, _VP, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats)],
+    "iemic_solver_gauge": [_VP, _IP, ctypes.c_int, _IP],
+    "iemic_get_solver_info": [_VP, ctypes.POINTER(SolverInfo)],
+    "iemic_kernel_timing": [_VP, ctypes.c_int],
+    "iemic_kernel_stats_get": [_VP, ctypes.c_int, ctypes.POINTER(KernelStats)],
+    "iemic_get_stream": [_VP, ctypes.POINTER(_VP)],
+    "iemic_default_newton_opts": [ctypes.POINTER(NewtonOpts)],
+    "iemic_newton": [_VP, _DP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonStats)],
+    "iemic_newton_dev": [_VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonStats)],
+    "iemic_default_continuation_opts": [ctypes.POINTER(ContinuationOpts)],
+    "iemic_continuation_run": [_VP, _DP, ctypes.POINTER(ContinuationOpts), ctypes.POINTER(ContinuationStats)],
+    "iemic_continuation_run_dev": [_VP, _VP, ctypes.POINTER(ContinuationOpts),
+                                   ctypes.POINTER(ContinuationStats)],
+    "iemic_launch_count": [],
 }
+_VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts"}
 
 _lib = None
 
@@ -105,7 +174,9 @@ def load_library(path=None, build_if_missing=True):
     for name, args in SIGNATURES.items():
         fn = getattr(L, name)
         fn.argtypes = args
-        fn.restype = None if name == "iemic_default_solve_opts" else ctypes.c_int
+        fn.restype = None if name in _VOID_RETURN else ctypes.c_int
+        if name == "iemic_launch_count":
+            fn.restype = ctypes.c_longlong
     if path == _build.LIB:
         _lib = L
     return L
@@ -269,6 +340,14 @@ class Ocean:
         self._check(self.L.iemic_apply_precon(self._h, precision, _dp(v), _dp(out)), "applyPrecon")
         return out
 
+    def getGauge(self):
+        """Pressure unknowns the solver holds at zero (gauge of J's null space)."""
+        cnt = ctypes.c_int()
+        self._check(self.L.iemic_solver_gauge(self._h, None, 0, ctypes.byref(cnt)), "getGauge")
+        out = np.zeros(max(cnt.value, 1), dtype=np.int32)
+        self._check(self.L.iemic_solver_gauge(self._h, _ip(out), cnt.value, ctypes.byref(cnt)), "getGauge")
+        return out[:cnt.value].copy()
+
     def solve(self, rhs=None, opts=None, **kw):
         """Ocean::solve: x = J^{-1} rhs (default rhs: the stored RHS)."""
         b = self.rhs if rhs is None else np.ascontiguousarray(rhs, dtype=np.float64)
@@ -285,3 +364,76 @@ class Ocean:
             raise IemicError(rc, "solve")
         self.sol[:] = x
         return x, stats
+
+    # ---- Newton and continuation (src/newton/Newton.H, src/continuation/Continuation.H)
+    def default_newton_opts(self, precision=PREC_MIXED):
+        o = NewtonOpts()
+        self.L.iemic_default_newton_opts(ctypes.byref(o))
+        o.solve.precision = precision
+        return o
+
+    def newton(self, x=None, opts=None, **kw):
+        """Newton iteration at fixed parameters from x (default: the stored state).
+        Returns (x, stats); the converged state also becomes the stored state."""
+        x = np.array(self.state if x is None else x, dtype=np.float64)
+        o = opts if opts is not None else self.default_newton_opts(kw.pop("precision", PREC_MIXED))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        st = NewtonStats()
+        rc = self.L.iemic_newton(self._h, _dp(x), ctypes.byref(o), ctypes.byref(st))
+        stats = _asdict(st)
+        stats["status"] = rc
+        if rc not in (0, -3):
+            raise IemicError(rc, "newton")
+        self.state[:] = x
+        return x, stats
+
+    def default_continuation_opts(self, par="Combined Forcing", precision=PREC_MIXED):
+        o = ContinuationOpts()
+        self.L.iemic_default_continuation_opts(ctypes.byref(o))
+        o.par_idx = self.par2int(par)
+        o.solve.precision = precision
+        return o
+
+    def continuation(self, x=None, opts=None, **kw):
+        """Continuation<Ocean>::run from x (default: the stored state).
+        Returns (x, stats) with stats["par"] the final parameter value."""
+        x = np.array(self.state if x is None else x, dtype=np.float64)
+        par = kw.pop("par", "Combined Forcing")
+        o = opts if opts is not None else self.default_continuation_opts(par, kw.pop("precision", PREC_MIXED))
+        for k, v in kw.items():
+            if k in ("residual_test", "normalize", "tangent", "initial_tangent") and isinstance(v, str):
+                v = v.encode()
+            setattr(o, k, v)
+        st = ContinuationStats()
+        rc = self.L.iemic_continuation_run(self._h, _dp(x), ctypes.byref(o), ctypes.byref(st))
+        stats = _asdict(st)
+        stats["status"] = rc
+        if rc not in (0, -3):
+            raise IemicError(rc, "continuation")
+        self.state[:] = x
+        return x, stats
+
+    def solverInfo(self):
+        """Size of the nested-dissection factorisation (fronts, entries, flops)."""
+        st = SolverInfo()
+        self._check(self.L.iemic_get_solver_info(self._h, ctypes.byref(st)), "solverInfo")
+        return _asdict(st)
+
+    # ---- device timing of the instrumented kernel classes -------------------
+    def kernelTiming(self, enable=True):
+        self._check(self.L.iemic_kernel_timing(self._h, 1 if enable else 0), "kernelTiming")
+
+    def kernelStats(self):
+        out = {}
+        for name, k in KERNEL_CLASSES.items():
+            st = KernelStats()
+            self._check(self.L.iemic_kernel_stats_get(self._h, k, ctypes.byref(st)), "kernelStats")
+            out[name] = _asdict(st)
+        return out
+
+    def stream(self):
+        """The cudaStream_t (as an int) all calls on this handle run on."""
+        p = _VP()
+        self._check(self.L.iemic_get_stream(self._h, ctypes.byref(p)), "stream")
+        return p.value or 0

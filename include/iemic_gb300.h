@@ -94,15 +94,17 @@ int iemic_mass(iemic_ocean* h, double* diagB);
 int iemic_apply_matrix(iemic_ocean* h, const double* v, double* out);
 
 /* Linear solve options / statistics (Ocean::solve, Ocean.C:1070-1147). */
-enum { IEMIC_PREC_FP64 = 0, IEMIC_PREC_MIXED = 1 };
+enum { IEMIC_PREC_FP64 = 0, IEMIC_PREC_MIXED = 1, IEMIC_PREC_FP32_KRYLOV = 2 };
 typedef struct {
     int precision;         /* IEMIC_PREC_FP64: FP64 GMRES + FP64 factors;
-                              IEMIC_PREC_MIXED: FP32 GMRES + FP32 factors inside FP64 refinement */
+                              IEMIC_PREC_MIXED: FP64 GMRES + FP32 factors (FP64-accumulated solves);
+                              IEMIC_PREC_FP32_KRYLOV: FP32 GMRES + FP32 factors inside FP64
+                              residual refinement (experimental) */
     int restart;           /* GMRES restart length ("FGMRES iterations") */
     int max_iters;         /* cap on total inner iterations */
     double tol;            /* relative residual target ||b - J x|| / ||b|| */
-    int max_refinements;   /* outer FP64 refinement steps (mixed only) */
-    double inner_tol;      /* FP32 inner relative tolerance (mixed only) */
+    int max_refinements;   /* outer FP64 refinement steps (FP32_KRYLOV only) */
+    double inner_tol;      /* FP32 inner relative tolerance (FP32_KRYLOV only) */
     int transpose;         /* 0: J x = b, 1: J^T x = b (adjoint solve) */
     int reuse_preconditioner; /* 0: refactor when J changed since the last factorisation;
                                  1: keep the existing factorisation (the reference recomputes its
@@ -124,11 +126,115 @@ void iemic_default_solve_opts(iemic_solve_opts* o);
 int iemic_build_preconditioner(iemic_ocean* h, int precision);
 /* Ocean::applyPrecon: out = M^{-1} v with the current factorisation. */
 int iemic_apply_precon(iemic_ocean* h, int precision, const double* v, double* out);
+/* The gauge of J's null space (no reference counterpart: the reference's
+ * Belos/Ifpack solve leaves it implicit). J is singular (hydrostatic B-grid
+ * pressure modes per basin); every solution the solver returns has exactly
+ * zero pressure at these unknowns, and their (redundant) continuity rows are
+ * satisfied through the others for consistent right-hand sides. With
+ * capacity 0 only *count is set. */
+int iemic_solver_gauge(iemic_ocean* h, int* idx, int capacity, int* count);
+/* Size of the preconditioner's nested-dissection factorisation (no
+ * reference counterpart). factor_entries: entries the triangular solves read
+ * (per precision multiply by 4 or 8 bytes); front_entries: dense front
+ * storage; factor_flops: flops of one factorisation. */
+typedef struct {
+    int64_t unknowns, reduced_unknowns, fronts, levels, factor_entries, front_entries;
+    double factor_flops;
+} iemic_solver_info;
+int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out);
 /* Ocean::solve(rhs): x = J^{-1} b (host vectors). */
 int iemic_solve(iemic_ocean* h, const double* b, double* x, const iemic_solve_opts* o,
                 iemic_solve_stats* st);
 int iemic_solve_dev(iemic_ocean* h, const double* b_dev, double* x_dev, const iemic_solve_opts* o,
                     iemic_solve_stats* st);
+
+/* Newton iteration at fixed parameters (Newton<Model>::Run / RunBackTracking,
+ * src/newton/Newton.H:40-100): x += dx with J dx = -F until ||F||_2 < tol,
+ * halving back-tracking whenever the residual norm grew. */
+typedef struct {
+    int max_iters;            /* maxNumIterations_ (10) */
+    double tol;               /* toleranceRHS_ on ||F||_2 (1e-3) */
+    int backtracking_steps;   /* numBackTrackingSteps_ (10) */
+    iemic_solve_opts solve;
+    int refactor_each_iter;   /* 1: new preconditioner every iteration */
+} iemic_newton_opts;
+typedef struct {
+    int iters, backtracks, linear_solves, krylov_iters, factorizations;
+    double rhs_norm0, rhs_norm;
+    double time_ms, time_assembly_ms, time_factor_ms, time_solve_ms;
+} iemic_newton_stats;
+void iemic_default_newton_opts(iemic_newton_opts* o);
+int iemic_newton(iemic_ocean* h, double* x, const iemic_newton_opts* o, iemic_newton_stats* st);
+int iemic_newton_dev(iemic_ocean* h, double* x_dev, const iemic_newton_opts* o, iemic_newton_stats* st);
+
+/* Pseudo-arclength continuation (Continuation<Model>::run,
+ * src/continuation/Continuation.H:209-1115). Field names follow the
+ * reference's "Continuation parameters" list; defaults
+ * (iemic_default_continuation_opts) are those of getDefaultInitParameters.
+ * The state advances in place; the model's parameter par_idx ends at the
+ * last accepted point. Returns IEMIC_ERR_NOT_CONVERGED when the run aborted
+ * at the minimum step size. */
+typedef struct {
+    int par_idx;              /* "continuation parameter": par(1..30), e.g. 15 "Salinity Forcing" */
+    double ds, ds_min, ds_max;/* "initial/minimum/maximum step size" */
+    double decrease;          /* "decrease step size": a failed step divides ds by it */
+    double destination;       /* "destination 0" */
+    double destination_tol;   /* "destination tolerance" */
+    int max_steps;            /* "maximum number of steps" (-1: until the destination) */
+    int max_newton;           /* "maximum Newton iterations" */
+    int min_newton;           /* "minimum Newton iterations" */
+    double opt_newton;        /* "optimal Newton iterations" (Seydel step control) */
+    double newton_tol;        /* "Newton tolerance" */
+    char residual_test;       /* "corrector residual test": 'R' ||F||_2, 'D' max(|dpar|, ||dx||_inf) */
+    char normalize;           /* "normalize strategy": 'O' or 'N' */
+    char tangent;             /* "tangent type": 'E' Euler, 'S' secant */
+    char initial_tangent;     /* "initial tangent type": 'E' (solve) or 'A' (-dF/dpar) */
+    double epsilon;           /* "epsilon increment" of the finite-difference dF/dpar */
+    double tan_scaling;       /* "state tangent scaling" */
+    double predictor_bound;   /* "predictor bound" on ||F||_2 */
+    int backtracking_steps;   /* "backtracking steps" (0: off) */
+    double backtracking_increase; /* "backtracking increase" */
+    int newton_chord;         /* "enable Newton Chord hybrid solve" */
+    int give_up_at_ds_min;    /* "give up at minimum step size" */
+    iemic_solve_opts solve;
+    int refactor_each_newton; /* 0: preconditioner rebuilt once per step (Ocean::preProcess);
+                                 1: rebuilt after every new Jacobian */
+} iemic_continuation_opts;
+typedef struct {
+    int steps, failed_steps, newton_iters, linear_solves, unconverged_solves, krylov_iters, factorizations;
+    int reached_destination, aborted;
+    double par, ds, rhs_norm;
+    double time_ms, time_assembly_ms, time_factor_ms, time_solve_ms;
+} iemic_continuation_stats;
+void iemic_default_continuation_opts(iemic_continuation_opts* o);
+int iemic_continuation_run(iemic_ocean* h, double* x, const iemic_continuation_opts* o,
+                           iemic_continuation_stats* st);
+int iemic_continuation_run_dev(iemic_ocean* h, double* x_dev, const iemic_continuation_opts* o,
+                               iemic_continuation_stats* st);
+
+/* Device timing of the instrumented kernel classes (no reference
+ * counterpart; it plays the role of the reference's TIMER_START/STOP
+ * profile, src/globaldefs/GlobalDefinitions.H:193-223). enable = 1 clears the
+ * counters and starts recording CUDA events around every launch of the
+ * classes below on the handle's stream; enable = 0 stops. bytes/flops are
+ * the launches' algorithmic bytes and flops. */
+enum {
+    IEMIC_KC_FACTOR_GEMM = 0,   /* trailing-update GEMM of the block LU */
+    IEMIC_KC_SOLVE_GEMV = 1,    /* triangular-solve GEMV sweeps of the preconditioner */
+    IEMIC_KC_ASSEMBLY = 2,      /* Jacobian / residual assembly */
+    IEMIC_KC_SPMV = 3,          /* CSR SpMV and residual of the Krylov solver */
+    IEMIC_KC_COUNT = 4
+};
+typedef struct {
+    long long launches;
+    double ms, bytes, flops;
+} iemic_kernel_stats;
+int iemic_kernel_timing(iemic_ocean* h, int enable);
+int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out);
+/* Kernel launches this library has made in the process so far. */
+long long iemic_launch_count(void);
+/* The CUDA stream (cudaStream_t) every call on this handle runs on. */
+int iemic_get_stream(iemic_ocean* h, void** stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,92 @@
+"""GPU linear solves against the oracle's exact solve in the same gauge.
+
+J x = b with b = -F(x_seeded) on the 16x16x4 box and a 24x12x6 periodic
+global ocean with seeded land: the GPU returns x with the FP64 residual
+||b - J x|| / ||b|| <= 1e-8 (the GMRES tolerance of Ocean::solve), zero
+pressure at its gauge unknowns, and agrees with the sparse-LU solution of the
+oracle's Jacobian in that gauge.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from helpers import box_case, global_case, make_gpu, make_oracle, seeded_state
+
+pytestmark = pytest.mark.gpu
+
+CASES = {"box": box_case, "glob24": global_case}
+
+
+def _setup(name, seed=0):
+    from oracle.continuation import OracleModel
+    cfg, lm, frc = CASES[name]()
+    g = make_gpu(cfg, lm, frc)
+    o = make_oracle(cfg, lm, frc)
+    x = seeded_state(cfg, seed)
+    F = g.computeRHS(x)
+    g.computeJacobian(x)
+    pins = g.getGauge()
+    M = OracleModel(o, pins)
+    M.jacobian(x)
+    return g, o, M, x, F, pins
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gauge_is_surface_pressure(name):
+    g, o, M, x, F, pins = _setup(name)
+    n, m, l = g.n, g.m, g.l
+    assert len(pins) >= 2
+    for p in pins:
+        assert p % 6 == 3                     # a pressure unknown
+        assert (p // 6) // (n * m) == l - 1   # in the surface layer
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_solve_matches_oracle(name, prec):
+    g, o, M, x, F, pins = _setup(name)
+    sol, st = g.solve(-F, precision=prec)
+    assert st["status"] == 0, st
+    J = M.J
+    relres = np.linalg.norm(J @ sol + F) / np.linalg.norm(F)
+    assert relres <= 1e-8 and st["relres"] <= 1e-8, (relres, st)
+    assert np.all(sol[pins] == 0.0)
+    ref = M.solve(-F)
+    err = np.linalg.norm(sol - ref) / np.linalg.norm(ref)
+    assert err <= 1e-5, err
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_preconditioner_is_an_exact_solve(name):
+    """The FP64 nested-dissection LU is a direct solver on the pinned system."""
+    g, o, M, x, F, pins = _setup(name)
+    g.buildPreconditioner(0)
+    z = g.applyPrecon(-F, precision=0)
+    ref = M.solve(-F)
+    assert np.linalg.norm(z - ref) / np.linalg.norm(ref) <= 1e-6
+
+
+def test_refactor_on_new_jacobian_and_reuse():
+    g, o, M, x, F, pins = _setup("box")
+    _, st1 = g.solve(-F, precision=1)
+    _, st2 = g.solve(-F, precision=1)
+    assert st1["factorizations"] == 1 and st2["factorizations"] == 0
+    # a nearby state: the kept factorisation still preconditions well
+    x2 = x + 1e-3 * seeded_state(g.config, 7)
+    F2 = g.computeRHS(x2)
+    g.computeJacobian(x2)
+    sol, st3 = g.solve(-F2, precision=1, reuse_preconditioner=1)
+    assert st3["factorizations"] == 0 and st3["relres"] <= 1e-8, st3
+    sol, st4 = g.solve(-F2, precision=1)
+    assert st4["factorizations"] == 1 and st4["relres"] <= 1e-8
+
+
+def test_zero_rhs_and_bad_arguments():
+    from iemic import IemicError
+    g, o, M, x, F, pins = _setup("box")
+    sol, st = g.solve(np.zeros(g.ndim), precision=0)
+    assert np.all(sol == 0) and st["iters"] == 0
+    with pytest.raises(IemicError):
+        g.solve(-F, precision=7)
+    with pytest.raises(IemicError):
+        g.solve(-F, precision=0, restart=0)
