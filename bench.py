@@ -45,7 +45,11 @@ def parse():
     ap.add_argument("--setup-comb", type=float, default=0.1)
     ap.add_argument("--fp64-steps", type=int, default=None, help="continuation steps of the FP64 comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     ap.add_argument("--cpu-iters", type=int, default=1, help="Newton iterations of the CPU sample")
+    ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1"],
+                    help="newton1: one Newton iteration per precision from the seeded state, per-kernel-class "
+                         "device times (a short case for profiling)")
     return ap.parse_args()
 
 
@@ -146,7 +150,8 @@ class Clocks:
 
 def roofline(stats, peaks):
     """Roofline of the dominant instrumented kernel class in the timed region."""
-    name, s = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    counted = {k: v for k, v in stats.items() if k in ("factor_gemm", "solve_gemv", "assembly", "spmv")}
+    name, s = max(counted.items(), key=lambda kv: kv[1]["ms"])
     avg_ms = s["ms"] / max(s["launches"], 1)
     out = {"kernel": name, "launches": s["launches"], "avg_launch_ms": avg_ms}
     if name == "factor_gemm":
@@ -288,7 +293,9 @@ def run_ours(args, rank, world):
     peaks = load_peaks()
     info = oc.solverInfo()
     results = {}
-    for label, prec, steps in (("mixed", 1, args.steps), ("fp64", 0, args.fp64_steps or args.steps)):
+    fp64_steps = args.steps if args.fp64_steps is None else args.fp64_steps
+    arms = [("mixed", 1, args.steps)] + ([("fp64", 0, fp64_steps)] if fp64_steps > 0 else [])
+    for label, prec, steps in arms:
         x = x_start.clone()
         oc.setPar("Salinity Forcing", par_w)
         torch.cuda.synchronize()
@@ -319,21 +326,26 @@ def run_ours(args, rank, world):
             results[label].update(launches=launches, clocks=clk, kstats=kstats)
 
     # --- end to end through the public API with host buffers (mixed path)
-    xh = x_start.cpu().numpy()
-    oc.setPar("Salinity Forcing", par_w)
-    o, kw = continuation_opts(oc, 1, args.steps, fscale)
-    kw["par"] = "Salinity Forcing"
-    kw["precision"] = 1
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    _, ste = oc.continuation(xh, **kw)
-    e2e_s = time.perf_counter() - t0
-    e2e_iters = barrier_sum(ste["newton_iters"], world)
-    e2e_s = barrier_max(e2e_s, world)
+    e2e = None
+    if not args.no_e2e:
+        xh = x_start.cpu().numpy()
+        oc.setPar("Salinity Forcing", par_w)
+        o, kw = continuation_opts(oc, 1, args.steps, fscale)
+        kw["par"] = "Salinity Forcing"
+        kw["precision"] = 1
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, ste = oc.continuation(xh, **kw)
+        e2e_s = time.perf_counter() - t0
+        e2e_iters = barrier_sum(ste["newton_iters"], world)
+        e2e_s = barrier_max(e2e_s, world)
+        e2e = {"value": e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * nd / args.steps,
+               "d2h_bytes_per_step": 8 * nd / args.steps,
+               "note": "one continuation call of %d steps with the state in host memory" % args.steps}
 
     if rank != 0:
         return
-    mixed, fp64 = results["mixed"], results["fp64"]
+    mixed, fp64 = results["mixed"], results.get("fp64")
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
@@ -349,14 +361,12 @@ def run_ours(args, rank, world):
         "newton_iters": mixed["newton_iters"], "continuation": {k: mixed["stats"][k] for k in (
             "steps", "failed_steps", "linear_solves", "krylov_iters", "factorizations", "par",
             "time_assembly_ms", "time_factor_ms", "time_solve_ms")},
-        "fp64_gpu": {"value": fp64["value"], "ms": fp64["ms"], "newton_iters": fp64["newton_iters"],
-                     "steps": fp64["stats"]["steps"], "krylov_iters": fp64["stats"]["krylov_iters"],
-                     "time_factor_ms": fp64["stats"]["time_factor_ms"],
-                     "time_solve_ms": fp64["stats"]["time_solve_ms"]},
-        "speedup_vs_fp64_gpu": mixed["value"] / fp64["value"],
-        "e2e": {"value": e2e_iters / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * nd / args.steps,
-                "d2h_bytes_per_step": 8 * nd / args.steps,
-                "note": "one continuation call of %d steps with the state in host memory" % args.steps},
+        "fp64_gpu": None if fp64 is None else {
+            "value": fp64["value"], "ms": fp64["ms"], "newton_iters": fp64["newton_iters"],
+            "steps": fp64["stats"]["steps"], "krylov_iters": fp64["stats"]["krylov_iters"],
+            "time_factor_ms": fp64["stats"]["time_factor_ms"], "time_solve_ms": fp64["stats"]["time_solve_ms"]},
+        "speedup_vs_fp64_gpu": None if fp64 is None else mixed["value"] / fp64["value"],
+        "e2e": e2e,
         "gpu_launches": mixed["launches"],
         "clocks": mixed["clocks"],
         "roofline": roofline(mixed["kstats"], peaks),
@@ -366,8 +376,43 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_newton1(args):
+    """One Newton iteration (J, F, F(par+eps), preconditioner, two solves) per
+    precision from the seeded rest state; per-kernel-class device times."""
+    import torch
+    from iemic import Ocean
+    from iemic import workloads as W
+    torch.cuda.init()
+    cfg, lm, frc = workload(args.workload)
+    oc = Ocean(cfg, lm, forcing=frc, starting_parameters=W.STARTING_PARAMETERS)
+    oc.setPar("Combined Forcing", args.setup_comb)
+    x = W.rest_state_with_ts_noise(cfg, 0)
+    out = {"mode": "newton1", "workload": args.workload, "solver": oc.solverInfo()}
+    for label, prec in (("mixed", 1), ("fp64", 0)):
+        for rep in range(2):            # the first pass builds the plan and allocates
+            oc.kernelTiming(True)
+            t0 = time.perf_counter()
+            F = oc.computeRHS(x)
+            oc.setPar("Salinity Forcing", oc.getPar("Salinity Forcing") + 1e-5)
+            Fe = oc.computeRHS(x)
+            oc.setPar("Salinity Forcing", oc.getPar("Salinity Forcing") - 1e-5)
+            oc.computeJacobian(x)
+            _, s1 = oc.solve((Fe - F) / 1e-5, precision=prec)
+            _, s2 = oc.solve(-F, precision=prec)
+            wall = time.perf_counter() - t0
+            ks = oc.kernelStats()
+            oc.kernelTiming(False)
+        out[label] = {"wall_s": wall, "solve1": s1, "solve2": s2,
+                      "classes_ms": {k: round(v["ms"], 3) for k, v in ks.items()},
+                      "launches": {k: v["launches"] for k, v in ks.items()}}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "newton1":
+        run_newton1(args)
+        return
     rank, world = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -913,7 +913,26 @@ __global__ void __launch_bounds__(NT) k_fwd_gather(const FrontDev* __restrict__ 
         }
     }
 }
-// partial GEMV products: forward rows [0,F) x own columns; backward own rows x [0,F)
+// Compensated (double-float) accumulation of a * (xh + xl) into (s, c) with
+// FP32 instructions only: the product's rounding error comes from an FMA and
+// the sum's from TwoSum (Knuth), so the result carries about 2 x 24 bits.
+// GB300 runs FP32 at 64x its FP64 rate, and FP32 factors applied with plain
+// FP32 sums lose the accuracy the refinement needs; this keeps FP64-level
+// accumulation at FP32 throughput. Intrinsics keep the compiler from fusing.
+__device__ __forceinline__ void dd_acc(float& s, float& c, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    float e = __fmaf_rn(a, xh, -p);
+    e = __fmaf_rn(a, xl, e);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+}
+
+// partial GEMV products: forward rows [0,F) x own columns; backward own rows x [0,F).
+// One thread per row of a (GR-row, GC-column) tile; partial sums go to the
+// forward (F x chunks) or backward (nf x chunks) partial buffer of the front.
 template <class T, bool BWD>
 __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
                                                   const T* __restrict__ front, const double* __restrict__ X,
@@ -924,30 +943,63 @@ __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ f
     const int r = it.row0 + threadIdx.x;
     const int nrows = BWD ? nf : F, ncols = BWD ? F : nf;
     __shared__ double xs[GC];
+    __shared__ float2 xs2[GC];
     const double* x = X + fr.woff;
-    for (int q = threadIdx.x; q < GC; q += GR) xs[q] = it.col0 + q < ncols ? x[it.col0 + q] : 0.0;
-    __syncthreads();
-    if (r >= nrows) return;
-    const T* A = front + fr.off;
-    double s = 0.0;
-    const int cend = min(ncols, it.col0 + GC);
-    if (!BWD) {
-        // rows < nf: Linv11 (lower, unit diagonal); rows >= nf: -G
-        if (r < nf) {
-            const int ce = min(cend, r);
-            for (int c = it.col0; c < ce; ++c) s += double(A[int64_t(c) * F + r]) * xs[c - it.col0];
-            if (r >= it.col0 && r < cend) s += xs[r - it.col0];
+    for (int q = threadIdx.x; q < GC; q += GR) {
+        const double v = it.col0 + q < ncols ? x[it.col0 + q] : 0.0;
+        if (sizeof(T) == 4) {
+            const float h = __double2float_rn(v);
+            xs2[q] = make_float2(h, __double2float_rn(v - double(h)));
         } else {
-            for (int c = it.col0; c < cend; ++c) s -= double(A[int64_t(c) * F + r]) * xs[c - it.col0];
-        }
-    } else {
-        // columns < nf: Uinv11 (upper incl. diagonal); columns >= nf: -H
-        for (int c = max(it.col0, r); c < cend; ++c) {
-            double a = double(A[int64_t(c) * F + r]);
-            s += c < nf ? a * xs[c - it.col0] : -a * xs[c - it.col0];
+            xs[q] = v;
         }
     }
-    part[part_off[it.front] + int64_t(it.chunk) * F + r] = s;
+    __syncthreads();
+    if (r >= nrows) return;
+    const T* A = front + fr.off + r;
+    const int cend = min(ncols, it.col0 + GC);
+    // [c0, c1) with sign +1, [c1, c2) with sign -1, plus the unit diagonal (forward, own rows)
+    int c0, c1, c2;
+    bool diag = false;
+    if (!BWD) {
+        if (r < nf) {
+            c0 = it.col0;
+            c1 = c2 = min(cend, r);
+            diag = r >= it.col0 && r < cend;
+        } else {
+            c0 = c1 = it.col0;
+            c2 = cend;
+        }
+    } else {
+        c0 = max(it.col0, r);
+        c1 = max(c0, min(cend, nf));
+        c2 = cend;
+    }
+    double out;
+    if (sizeof(T) == 4) {
+        float sh = 0.f, sl = 0.f;
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) {
+            const float2 xv = xs2[c - it.col0];
+            dd_acc(sh, sl, float(A[int64_t(c) * F]), xv.x, xv.y);
+        }
+#pragma unroll 4
+        for (int c = c1; c < c2; ++c) {
+            const float2 xv = xs2[c - it.col0];
+            dd_acc(sh, sl, -float(A[int64_t(c) * F]), xv.x, xv.y);
+        }
+        out = double(sh) + double(sl);
+        if (diag) out += xs2[r - it.col0].x + double(xs2[r - it.col0].y);
+    } else {
+        double acc = 0.0;
+#pragma unroll 4
+        for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * F]) * xs[c - it.col0];
+#pragma unroll 4
+        for (int c = c1; c < c2; ++c) acc -= double(A[int64_t(c) * F]) * xs[c - it.col0];
+        out = acc;
+        if (diag) out += xs[r - it.col0];
+    }
+    part[part_off[it.front] + int64_t(it.chunk) * nrows + r] = out;
 }
 // forward epilogue: own rows -> y (kept in W), boundary rows -> update vector in WP
 __global__ void k_fwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
@@ -980,7 +1032,7 @@ __global__ void k_bwd_reduce(const FrontDev* __restrict__ fronts, const int* __r
     if (r >= fr.nf) return;
     const int nch = (fr.F + GC - 1) / GC;
     double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.F + r];
+    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.nf + r];
     xred[fr.red0 + r] = s;
 }
 
@@ -1071,12 +1123,14 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_wp = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
     // solve-phase work items and partial-sum offsets
     std::vector<WorkItem> fi, bi;
-    std::vector<int64_t> part_off(plan.nfronts, 0);
-    int64_t poff = 0;
+    std::vector<int64_t> part_off(plan.nfronts, 0), part_off_b(plan.nfronts, 0);
+    int64_t poff = 0, poff_b = 0;
     for (int f = 0; f < plan.nfronts; ++f) {
         const FrontDev& fr = plan.fronts[f];
         part_off[f] = poff;
-        poff += int64_t(fr.F) * ((fr.F + GC - 1) / GC);
+        poff += int64_t(fr.F) * ((fr.nf + GC - 1) / GC);
+        part_off_b[f] = poff_b;
+        poff_b += int64_t(fr.nf) * ((fr.F + GC - 1) / GC);
     }
     lu.fwd_items_start.clear();
     lu.bwd_items_start.clear();
@@ -1091,10 +1145,14 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
             // forward: strict lower Linv11 + G (nb x nf); backward: upper Uinv11 + H (nf x nb)
             lu.fwd_bytes[h] += double(ts) * (nf * (nf - 1) / 2 + nb * nf);
             lu.bwd_bytes[h] += double(ts) * (nf * (nf + 1) / 2 + nf * nb);
+            // tiles that hold no entry of the triangular parts are skipped (their
+            // partial sums stay at the zero they are initialised to)
             for (int c = 0; c * GC < fr.nf; ++c)
-                for (int r = 0; r * GR < fr.F; ++r) fi.push_back(WorkItem{f, r * GR, c * GC, c});
+                for (int r = 0; r * GR < fr.F; ++r)
+                    if (!(r * GR + GR <= fr.nf && c * GC >= r * GR + GR)) fi.push_back(WorkItem{f, r * GR, c * GC, c});
             for (int c = 0; c * GC < fr.F; ++c)
-                for (int r = 0; r * GR < fr.nf; ++r) bi.push_back(WorkItem{f, r * GR, c * GC, c});
+                for (int r = 0; r * GR < fr.nf; ++r)
+                    if (!(c * GC + GC <= r * GR)) bi.push_back(WorkItem{f, r * GR, c * GC, c});
         }
     }
     lu.fwd_items_start.push_back(int(fi.size()));
@@ -1103,6 +1161,10 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_bwd_items = upload(lu, bi, s);
     lu.d_part_off = upload(lu, part_off, s);
     lu.d_part = dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(poff, 1)));
+    ck(cudaMemsetAsync(lu.d_part, 0, sizeof(double) * size_t(std::max<int64_t>(poff, 1)), s));
+    lu.d_part_off_b = upload(lu, part_off_b, s);
+    lu.d_part_b = dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(poff_b, 1)));
+    ck(cudaMemsetAsync(lu.d_part_b, 0, sizeof(double) * size_t(std::max<int64_t>(poff_b, 1)), s));
     // factorisation scratch (per level, per front)
     std::vector<int64_t> sct, scg;
     int64_t mx = 0;
@@ -1144,15 +1206,18 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
     T* dinv = static_cast<T*>(lu.d_dinv);
     T* scratch = static_cast<T*>(lu.d_scratch);
     const T tau = sizeof(T) == 4 ? T(1e-7) : T(1e-15);
+    cudaEvent_t ev_fs = lu.timer ? lu.timer->start(s) : nullptr;
     equilibrate(lu, rp, ci, values, s);
     ck(cudaMemsetAsync(front, 0, sizeof(T) * size_t(P.front_entries), s));
     ck(cudaMemsetAsync(lu.d_npert, 0, sizeof(int), s));
     const int64_t na = int64_t(P.asm_src.size());
     k_assemble<T><<<blocks_for(na), NT, 0, s>>>(na, lu.d_asm_src, lu.d_asm_dst, lu.d_asm_row, ci, values, lu.d_dr,
                                                 lu.d_dc, front); IEMIC_COUNT_LAUNCH();
+    if (ev_fs) lu.timer->stop(ev_fs, s, IEMIC_KC_FACTOR_SETUP, 0.0, 0.0);
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
+        cudaEvent_t ev_ea = lu.timer ? lu.timer->start(s) : nullptr;
         for (int sl = 0; sl < 2; ++sl) {
             int nc = lu.child_start[sl][h + 1] - lu.child_start[sl][h];
             if (nc == 0) continue;
@@ -1162,13 +1227,16 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
             k_extend_add<T><<<g, NT, 0, s>>>(lu.d_fronts, lu.d_level_children[sl] + lu.child_start[sl][h], lu.d_emap,
                                              front); IEMIC_COUNT_LAUNCH();
         }
+        if (ev_ea) lu.timer->stop(ev_ea, s, IEMIC_KC_FACTOR_SETUP, 0.0, 0.0);
         const int maxnf = P.level_maxnf[h], maxF = P.level_maxF[h];
         for (int p = 0; p < maxnf; p += B) {
+            cudaEvent_t ev_pn = lu.timer ? lu.timer->start(s) : nullptr;
             k_panel_diag<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert); IEMIC_COUNT_LAUNCH();
             dim3 g1((maxF + NT - 1) / NT, nfr);
             k_rowperm_u12<T, B><<<g1, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv); IEMIC_COUNT_LAUNCH();
             dim3 g3((maxF - p + NT - 1) / NT, nfr);
             k_l21<T, B><<<g3, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv); IEMIC_COUNT_LAUNCH();
+            if (ev_pn) lu.timer->stop(ev_pn, s, IEMIC_KC_FACTOR_PANEL, 0.0, 0.0);
             const int tiles = (maxF - p + 63) / 64;
             dim3 g2(tiles * tiles, nfr);
             cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
@@ -1189,6 +1257,7 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
         const int maxblk = (maxnf + B - 1) / B;
         const int64_t* sct = lu.d_sc_tr + lu.level_start[h];
         const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
+        cudaEvent_t ev_inv = lu.timer ? lu.timer->start(s) : nullptr;
         k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
         const int ctiles = (maxnf + 63) / 64;
         const int cblocks = blocks_for(int64_t(maxnf) * B);
@@ -1212,6 +1281,7 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
             k_gh<T, true><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
             k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
         }
+        if (ev_inv) lu.timer->stop(ev_inv, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
     }
     ck(cudaGetLastError());
     ck(cudaMemcpyAsync(&lu.npert, lu.d_npert, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1230,12 +1300,20 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
     double* W = static_cast<double*>(lu.d_w);
     double* WP = static_cast<double*>(lu.d_wp);
     double* part = static_cast<double*>(lu.d_part);
+    double* part_b = static_cast<double*>(lu.d_part_b);
     const T* front = static_cast<const T*>(lu.d_front);
+    KTimer* kt = lu.timer;
+    cudaEvent_t ev_so = kt ? kt->start(s) : nullptr;
     k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
+    if (ev_so) kt->stop(ev_so, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
-        k_fwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
+        {
+            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            k_fwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
+            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
         const int ni = lu.fwd_items_start[h + 1] - lu.fwd_items_start[h];
         cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
         if (ni) {
@@ -1243,24 +1321,40 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
                                                         lu.fwd_items_start[h], front, WP, part, lu.d_part_off); IEMIC_COUNT_LAUNCH();
         }
         if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.fwd_bytes[h], 2.0 * lu.fwd_bytes[h] / sizeof(T));
-        k_fwd_reduce<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off, W,
-                                                                                WP); IEMIC_COUNT_LAUNCH();
+        {
+            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            k_fwd_reduce<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off, W,
+                                                                                    WP); IEMIC_COUNT_LAUNCH();
+            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
     }
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
-        k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
+        {
+            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
+            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
         const int ni = lu.bwd_items_start[h + 1] - lu.bwd_items_start[h];
         cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
         if (ni) {
             k_gemv_part<T, true><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_bwd_items) +
-                                                       lu.bwd_items_start[h], front, WP, part, lu.d_part_off); IEMIC_COUNT_LAUNCH();
+                                                       lu.bwd_items_start[h], front, WP, part_b, lu.d_part_off_b); IEMIC_COUNT_LAUNCH();
         }
         if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.bwd_bytes[h], 2.0 * lu.bwd_bytes[h] / sizeof(T));
-        k_bwd_reduce<<<dim3((P.level_maxnf[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off,
-                                                                                 red); IEMIC_COUNT_LAUNCH();
+        {
+            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            k_bwd_reduce<<<dim3((P.level_maxnf[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part_b, lu.d_part_off_b,
+                                                                                     red); IEMIC_COUNT_LAUNCH();
+            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
     }
-    k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dc, red, r, z); IEMIC_COUNT_LAUNCH();
+    {
+        cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+        k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dc, red, r, z); IEMIC_COUNT_LAUNCH();
+        if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+    }
     ck(cudaGetLastError());
 }
 

@@ -72,8 +72,10 @@ struct NdLu {
     void* d_red = nullptr;                  // reduced rhs / solution (T)
     int* d_npert = nullptr;                 // perturbed-pivot counter
     void* d_wp = nullptr;                   // permuted / gathered solve vectors (FP64)
-    void* d_part = nullptr;                 // GEMV partial sums (FP64)
+    void* d_part = nullptr;                 // forward GEMV partial sums (FP64), F x chunks per front
     int64_t* d_part_off = nullptr;
+    void* d_part_b = nullptr;               // backward GEMV partial sums (FP64), nf x chunks per front
+    int64_t* d_part_off_b = nullptr;
     void *d_fwd_items = nullptr, *d_bwd_items = nullptr;   // GEMV work items per level
     std::vector<int> fwd_items_start, bwd_items_start;
     int64_t *d_sc_tr = nullptr, *d_sc_gh = nullptr;         // scratch offsets per front (by level)

@@ -110,7 +110,8 @@ class SolverInfo(ctypes.Structure):
                 ("factor_flops", ctypes.c_double)]
 
 
-KERNEL_CLASSES = {"factor_gemm": 0, "solve_gemv": 1, "assembly": 2, "spmv": 3}
+KERNEL_CLASSES = {"factor_gemm": 0, "solve_gemv": 1, "assembly": 2, "spmv": 3, "factor_panel": 4,
+                  "factor_inverse": 5, "factor_setup": 6, "solve_other": 7}
 
 
 def _asdict(st):

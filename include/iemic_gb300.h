@@ -223,7 +223,11 @@ enum {
     IEMIC_KC_SOLVE_GEMV = 1,    /* triangular-solve GEMV sweeps of the preconditioner */
     IEMIC_KC_ASSEMBLY = 2,      /* Jacobian / residual assembly */
     IEMIC_KC_SPMV = 3,          /* CSR SpMV and residual of the Krylov solver */
-    IEMIC_KC_COUNT = 4
+    IEMIC_KC_FACTOR_PANEL = 4,  /* panel LU, row permutations and L21 of the block LU */
+    IEMIC_KC_FACTOR_INVERSE = 5,/* explicit triangular inverses and G, H of the fronts */
+    IEMIC_KC_FACTOR_SETUP = 6,  /* equilibration, front assembly and extend-add */
+    IEMIC_KC_SOLVE_OTHER = 7,   /* gathers, reductions and scatter of the triangular solves */
+    IEMIC_KC_COUNT = 8
 };
 typedef struct {
     long long launches;
