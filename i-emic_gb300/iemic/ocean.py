@@ -133,6 +133,7 @@ SIGNATURES = {
     "iemic_rhs": [_VP, _DP, _DP],
     "iemic_jacobian": [_VP, _DP],
     "iemic_rhs_dev": [_VP, _VP, _VP],
+    "iemic_rhs_dev_noalloc": [_VP, _VP, _VP],
     "iemic_jacobian_dev": [_VP, _VP],
     "iemic_graph_nnz": [_VP, ctypes.POINTER(ctypes.c_int64)],
     "iemic_get_csr": [_VP, _IP, _IP, _DP, ctypes.c_int],

@@ -85,6 +85,16 @@ int iemic_jacobian(iemic_ocean* h, const double* x);
 int iemic_rhs_dev(iemic_ocean* h, const double* x_dev, double* F_dev);
 int iemic_jacobian_dev(iemic_ocean* h, const double* x_dev);
 
+/* iemic_rhs_dev without per-handle scratch (no reference counterpart): the
+ * padded state fields live in one static device array of
+ * IEMIC_NOALLOC_MAX_PADDED_CELLS cells per field; grids with
+ * (n+2)(m+2)(l+2) above it are rejected (IEMIC_ERR_ARG). Allocates nothing.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and must
+ * not run during stream capture. Calls overlapping in time on one device race
+ * on the shared array. Runs on the handle's stream like iemic_rhs_dev. */
+#define IEMIC_NOALLOC_MAX_PADDED_CELLS 65536
+int iemic_rhs_dev_noalloc(iemic_ocean* h, const double* x_dev, double* F_dev);
+
 /* Ocean::getJacobian: the CSR of the maximal graph, 0- or 1-based. */
 int iemic_graph_nnz(const iemic_ocean* h, int64_t* nnz);
 int iemic_get_csr(iemic_ocean* h, int* row_ptr, int* col_idx, double* values, int index_base);
