@@ -650,9 +650,14 @@ __global__ void __launch_bounds__(256) k_gemm(const FrontDev* __restrict__ front
 
 // ---------------------------------------------------------------------------
 // explicit inverses for the solve phase: after its LU, every front holds
-//   Linv11 (strict lower part, unit diagonal), Uinv11 (upper part),
-//   G = L21 * Linv11 in place of L21 and H = Uinv11 * U12 in place of U12,
-// so forward and backward substitution become one GEMV per level.
+//   Linv11 (strict lower part, unit diagonal) and Uinv11 (upper part) in place
+//   of L11 and U11, so the triangular solves become dense GEMVs. FP32 factors
+//   also replace L21 by G = L21 * Linv11 and U12 by H = Uinv11 * U12, so both
+//   blocks of a sweep read the same input vector and one GEMV launch per
+//   level and sweep does the work (their solves run ~30 times per
+//   factorisation); FP64 factors keep L21 and U12 and run two dependent GEMV
+//   stages per level and sweep, because on GB300's FP64 pipe forming G and H
+//   costs more than the few extra launches of their handful of solves.
 // ---------------------------------------------------------------------------
 enum { MD_DENSE = 0, MD_LOWER_UNIT = 1, MD_UPPER = 2 };
 template <class T, int MODE>
@@ -678,82 +683,92 @@ __global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* _
     }
 }
 
-// One block-row step of the blocked triangular inversions, into scratch:
-//   LOWER (step i >= 1):  X[Ri, 0:iB]  = -Linv_ii * (L[Ri, 0:iB] * X[0:iB, 0:iB])
-//   UPPER (step i):       Y[Ri, iB+bb:nf] = -Uinv_ii * (U[Ri, iB+bb:nf] * Y[iB+bb:nf, iB+bb:nf])
-// One CTA per (front, 64-column tile); bb <= B <= 32 rows.
-template <class T, int B, bool UPPER>
-__global__ void __launch_bounds__(256) k_trinv_step(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                                    int i, T* __restrict__ front, const T* __restrict__ dinv,
-                                                    T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
-    const FrontDev fr = fronts[lf[blockIdx.y]];
-    const int nblk = (fr.nf + B - 1) / B;
-    if (i >= nblk || (!UPPER && i == 0)) return;
-    const int r0 = i * B, bb = min(B, fr.nf - r0), F = fr.F;
-    const int cbeg = UPPER ? r0 + bb : 0, cend = UPPER ? fr.nf : r0;
-    const int c0 = cbeg + blockIdx.x * 64;
-    if (c0 >= cend) return;
-    const T* A = front + fr.off;
-    __shared__ T As[B][33];     // A[r0 + rr, k0 + kk]
-    __shared__ T Xs[32][65];    // X[k0 + kk, c0 + cc]
-    __shared__ T Ts[B][65];
-    const int tid = threadIdx.x, cc = tid % 64, rq = tid / 64;   // 4 row groups
-    T acc[8];
+// Triangular inversion in two parts, all fronts of a level and both triangles
+// in the same launches, each step two batched GEMMs (a product into scratch,
+// then the second product in place):
+//  (1) inside every 256-row super-block, pairs of neighbouring inverted
+//      diagonal blocks A (first) and D (second) of size s = 32, 64, 128 merge:
+//        lower:  X21 = -Dinv * (L21blk * Ainv)    upper:  X12 = -(Ainv * U12blk) * Dinv
+//  (2) over the super-blocks, block-row steps of the row-oriented method
+//      (lower top down, upper bottom up), whose rounding errors carry one
+//      large inverse per product instead of the two of a merge (Du Croz and
+//      Higham, IMA J. Numer. Anal. 12 (1992) 1-19), which the FP32
+//      preconditioner's quality depends on for ill-conditioned factors.
+// Triangular operands are read in place through masks (unit lower / upper)
+// and the K loop skips their zero part.
+enum { OP_DENSE = 0, OP_LOWER_UNIT = 1, OP_UPPER = 2 };
+constexpr int TRI_SB = 256;   // super-block rows of the row-oriented steps
+struct TriTask {
+    int64_t a_off, b_off, c_off;   // element offsets: base 0 = front storage, 1 = scratch
+    int lda, ldb, ldc, M, N, K;
+    int opA, opB, a_base, b_base, c_base;
+    float alpha;
+};
+struct TriTile {
+    int task, i0, j0;
+};
+template <class T>
+__device__ __forceinline__ T tri_ld(const T* P, int ld, int r, int c, int op) {
+    if (op == OP_LOWER_UNIT) return r > c ? P[int64_t(c) * ld + r] : (r == c ? T(1) : T(0));
+    if (op == OP_UPPER) return r <= c ? P[int64_t(c) * ld + r] : T(0);
+    return P[int64_t(c) * ld + r];
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_tri_gemm(const TriTask* __restrict__ tasks, const TriTile* __restrict__ tiles,
+                                                  T* __restrict__ front, T* __restrict__ scr) {
+    const TriTile tl = tiles[blockIdx.x];
+    const TriTask t = tasks[tl.task];
+    const T* A = (t.a_base ? scr : front) + t.a_off;
+    const T* Bm = (t.b_base ? scr : front) + t.b_off;
+    T* C = (t.c_base ? scr : front) + t.c_off;
+    const int i0 = tl.i0, j0 = tl.j0;
+    int kb = 0, ke = t.K;
+    if (t.opA == OP_LOWER_UNIT) ke = min(ke, i0 + 64);
+    if (t.opA == OP_UPPER) kb = max(kb, i0);
+    if (t.opB == OP_LOWER_UNIT) kb = max(kb, j0);
+    if (t.opB == OP_UPPER) ke = min(ke, j0 + 64);
+    __shared__ T As[32][65];
+    __shared__ T Bs[32][65];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    T acc[4][4];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q] = T(0);
-    // k range: LOWER: [c0, r0) (X lower: k >= c); UPPER: [cbeg, min(cend, c0 + 64))
-    const int kb = UPPER ? cbeg : c0, ke = UPPER ? min(cend, c0 + 64) : r0;
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
     for (int k0 = kb; k0 < ke; k0 += 32) {
-        for (int e = tid; e < B * 32; e += 256) {
-            int rr = e % B, kk = e / B;
-            As[rr][kk] = (rr < bb && k0 + kk < ke) ? A[int64_t(k0 + kk) * F + r0 + rr] : T(0);
+        for (int e = tid; e < 32 * 64; e += 256) {
+            const int ii = e % 64, kk = e / 64, r = i0 + ii, k = k0 + kk;
+            As[kk][ii] = (r < t.M && k < ke) ? tri_ld(A, t.lda, r, k, t.opA) : T(0);
         }
         for (int e = tid; e < 32 * 64; e += 256) {
-            int kk = e % 32, c = e / 32;
-            int gk = k0 + kk, gc = c0 + c;
-            T v = T(0);
-            if (gk < ke && gc < cend)
-                v = UPPER ? opld<T, MD_UPPER>(A, F, gk, gc) : opld<T, MD_LOWER_UNIT>(A, F, gk, gc);
-            Xs[kk][c] = v;
+            const int kk = e % 32, jj = e / 32, k = k0 + kk, c = j0 + jj;
+            Bs[kk][jj] = (c < t.N && k < ke) ? tri_ld(Bm, t.ldb, k, c, t.opB) : T(0);
         }
         __syncthreads();
 #pragma unroll 8
         for (int kk = 0; kk < 32; ++kk) {
-            T xv = Xs[kk][cc];
+            T av[4], bv[4];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) acc[q] += As[rq * 8 + q][kk] * xv;
+            for (int a = 0; a < 4; ++a) av[a] = As[kk][tx * 4 + a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][ty * 4 + b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
         }
         __syncthreads();
     }
+    const T alpha = T(t.alpha);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) Ts[rq * 8 + q][cc] = acc[q];
-    __syncthreads();
-    const T* Di = dinv + fr.dinv_off + int64_t(i) * 2 * B * B + (UPPER ? B * B : 0);
-    T* S = scratch + sc_off[blockIdx.y];
-    if (c0 + cc < cend) {
-        for (int q = 0; q < 8; ++q) {
-            int r = rq * 8 + q;
-            if (r >= bb) continue;
-            T sum = T(0);
-            for (int t = 0; t < bb; ++t) sum += Di[r * B + t] * Ts[t][cc];
-            S[int64_t(c0 + cc - cbeg) * B + r] = -sum;
+    for (int b = 0; b < 4; ++b) {
+        const int c = j0 + ty * 4 + b;
+        if (c >= t.N) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = i0 + tx * 4 + a;
+            if (r < t.M) C[int64_t(c) * t.ldc + r] = alpha * acc[a][b];
         }
-    }
-}
-template <class T, int B, bool UPPER>
-__global__ void k_trinv_copy(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int i,
-                             T* __restrict__ front, const T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
-    const FrontDev fr = fronts[lf[blockIdx.y]];
-    const int nblk = (fr.nf + B - 1) / B;
-    if (i >= nblk || (!UPPER && i == 0)) return;
-    const int r0 = i * B, bb = min(B, fr.nf - r0);
-    const int cbeg = UPPER ? r0 + bb : 0, cend = UPPER ? fr.nf : r0;
-    const int64_t tot = int64_t(cend - cbeg) * bb;
-    const T* S = scratch + sc_off[blockIdx.y];
-    T* A = front + fr.off;
-    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
-        int r = int(e % bb), c = int(e / bb);
-        A[int64_t(cbeg + c) * fr.F + r0 + r] = S[int64_t(c) * B + r];
     }
 }
 
@@ -874,13 +889,28 @@ __global__ void k_expand(int ndim, const int* __restrict__ g2r, const char* __re
 }
 
 // Solve phase, one level at a time (all fronts of the level together).
-// Work items split every front into (256-row tile, 256-column chunk) pieces
+// With L21/U12 (FP64 factors), two GEMV stages per level and sweep:
+//   forward:  y = Linv11 (P w_own);           u_B = w_B - L21 y
+//   backward: t = y - U12 x_B;                x_own = Uinv11 t
+// With G/H (FP32 factors), one fused launch per level and sweep:
+//   forward:  y = Linv11 (P w_own), u_B = w_B - G (P w_own)
+//   backward: x_own = Uinv11 y - H x_B
+// Work items split every block into (256-row tile, 256-column chunk) pieces
 // so the GEMVs spread over all SMs; partial sums per chunk are reduced in a
-// second pass (deterministic order). Accumulation is FP64.
+// second pass (deterministic order), each stage into its own zero-initialised
+// buffer so that skipped empty tiles contribute exact zeros.
 struct WorkItem {
-    int front, row0, col0, chunk;
+    int front, row0, col0, chunk, stage;
 };
 constexpr int GR = 256, GC = 256;
+enum { ST_LINV = 0, ST_UINV = 1, ST_L21 = 2, ST_U12 = 3, NSTAGE = 4 };
+// rows and columns of a stage's block inside a front
+__host__ __device__ inline void stage_block(int st, int nf, int F, int& r0, int& r1, int& c0, int& c1) {
+    r0 = st == ST_L21 ? nf : 0;
+    r1 = st == ST_L21 ? F : nf;
+    c0 = st == ST_U12 ? nf : 0;
+    c1 = st == ST_U12 ? F : nf;
+}
 
 // forward prologue: w = [red_C ; 0] + children's update vectors, then the
 // block-local row permutations applied to the own part (into wp)
@@ -930,23 +960,28 @@ __device__ __forceinline__ void dd_acc(float& s, float& c, float a, float xh, fl
     c = __fadd_rn(c, __fadd_rn(err, e));
 }
 
-// partial GEMV products: forward rows [0,F) x own columns; backward own rows x [0,F).
-// One thread per row of a (GR-row, GC-column) tile; partial sums go to the
-// forward (F x chunks) or backward (nf x chunks) partial buffer of the front.
-template <class T, bool BWD>
-__global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
-                                                  const T* __restrict__ front, const double* __restrict__ X,
-                                                  double* __restrict__ part, const int64_t* __restrict__ part_off) {
-    const WorkItem it = items[blockIdx.x];
-    const FrontDev fr = fronts[it.front];
+// Partial GEMV products of one stage: thread per row of a (GR-row, GC-column)
+// tile; ST_LINV uses the strict lower part plus the unit diagonal, ST_UINV the
+// upper part, ST_L21 and ST_U12 the dense blocks with a minus sign. Partial
+// sums go to part[off + chunk * rows + (r - r0)].
+struct StageBufs {
+    double* part[4];
+    const int64_t* off[4];
+};
+template <class T, int ST>
+__device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& fr, const T* __restrict__ front,
+                                           const double* __restrict__ X, const StageBufs& sb) {
+    double* __restrict__ part = sb.part[ST];
+    const int64_t* __restrict__ part_off = sb.off[ST];
     const int F = fr.F, nf = fr.nf;
+    int br0, br1, bc0, bc1;
+    stage_block(ST, nf, F, br0, br1, bc0, bc1);
     const int r = it.row0 + threadIdx.x;
-    const int nrows = BWD ? nf : F, ncols = BWD ? F : nf;
     __shared__ double xs[GC];
     __shared__ float2 xs2[GC];
     const double* x = X + fr.woff;
     for (int q = threadIdx.x; q < GC; q += GR) {
-        const double v = it.col0 + q < ncols ? x[it.col0 + q] : 0.0;
+        const double v = it.col0 + q < bc1 ? x[it.col0 + q] : 0.0;
         if (sizeof(T) == 4) {
             const float h = __double2float_rn(v);
             xs2[q] = make_float2(h, __double2float_rn(v - double(h)));
@@ -955,38 +990,25 @@ __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ f
         }
     }
     __syncthreads();
-    if (r >= nrows) return;
+    if (r >= br1) return;
     const T* A = front + fr.off + r;
-    const int cend = min(ncols, it.col0 + GC);
-    // [c0, c1) with sign +1, [c1, c2) with sign -1, plus the unit diagonal (forward, own rows)
-    int c0, c1, c2;
+    const int cend = min(bc1, it.col0 + GC);
+    int c0 = it.col0, c1 = cend;
     bool diag = false;
-    if (!BWD) {
-        if (r < nf) {
-            c0 = it.col0;
-            c1 = c2 = min(cend, r);
-            diag = r >= it.col0 && r < cend;
-        } else {
-            c0 = c1 = it.col0;
-            c2 = cend;
-        }
-    } else {
+    if (ST == ST_LINV) {
+        c1 = min(cend, r);
+        diag = r >= it.col0 && r < cend;
+    } else if (ST == ST_UINV) {
         c0 = max(it.col0, r);
-        c1 = max(c0, min(cend, nf));
-        c2 = cend;
     }
+    const float sg = (ST == ST_L21 || ST == ST_U12) ? -1.f : 1.f;
     double out;
     if (sizeof(T) == 4) {
         float sh = 0.f, sl = 0.f;
 #pragma unroll 4
         for (int c = c0; c < c1; ++c) {
             const float2 xv = xs2[c - it.col0];
-            dd_acc(sh, sl, float(A[int64_t(c) * F]), xv.x, xv.y);
-        }
-#pragma unroll 4
-        for (int c = c1; c < c2; ++c) {
-            const float2 xv = xs2[c - it.col0];
-            dd_acc(sh, sl, -float(A[int64_t(c) * F]), xv.x, xv.y);
+            dd_acc(sh, sl, sg * float(A[int64_t(c) * F]), xv.x, xv.y);
         }
         out = double(sh) + double(sl);
         if (diag) out += xs2[r - it.col0].x + double(xs2[r - it.col0].y);
@@ -994,27 +1016,77 @@ __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ f
         double acc = 0.0;
 #pragma unroll 4
         for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * F]) * xs[c - it.col0];
-#pragma unroll 4
-        for (int c = c1; c < c2; ++c) acc -= double(A[int64_t(c) * F]) * xs[c - it.col0];
-        out = acc;
+        out = double(sg) * acc;
         if (diag) out += xs[r - it.col0];
     }
-    part[part_off[it.front] + int64_t(it.chunk) * nrows + r] = out;
+    part[part_off[it.front] + int64_t(it.chunk) * (br1 - br0) + (r - br0)] = out;
 }
-// forward epilogue: own rows -> y (kept in W), boundary rows -> update vector in WP
-__global__ void k_fwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                             const double* __restrict__ part, const int64_t* __restrict__ part_off,
-                             double* __restrict__ W, double* __restrict__ WP) {
+template <class T>
+__global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
+                                                  const T* __restrict__ front, const double* __restrict__ X, StageBufs sb) {
+    const WorkItem it = items[blockIdx.x];
+    const FrontDev fr = fronts[it.front];
+    switch (it.stage) {
+        case ST_LINV: gemv_stage<T, ST_LINV>(it, fr, front, X, sb); break;
+        case ST_UINV: gemv_stage<T, ST_UINV>(it, fr, front, X, sb); break;
+        case ST_L21: gemv_stage<T, ST_L21>(it, fr, front, X, sb); break;
+        default: gemv_stage<T, ST_U12>(it, fr, front, X, sb); break;
+    }
+}
+
+// Stage epilogues (one thread per row of the stage's block):
+//   ST_LINV: y -> W (kept for the backward sweep) and WP (input of ST_L21)
+//   ST_L21:  WP[B] += partials (the update vector u_B for the parent)
+//   ST_U12:  WP[own] = y + partials (t)
+//   ST_UINV: x_own -> xred
+__device__ __forceinline__ double stage_sum(int st, int f, const FrontDev& fr, int r, const StageBufs& sb) {
+    int br0, br1, bc0, bc1;
+    stage_block(st, fr.nf, fr.F, br0, br1, bc0, bc1);
+    const int rows = br1 - br0, nch = (bc1 - bc0 + GC - 1) / GC;
+    const double* p = sb.part[st] + sb.off[st][f] + (r - br0);
+    double s = 0.0;
+    for (int c = 0; c < nch; ++c) s += p[int64_t(c) * rows];
+    return s;
+}
+// fused epilogues of the G/H layout: forward rows [0, F), backward rows [0, nf)
+template <bool BWD>
+__global__ void k_fused_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
+                               double* __restrict__ W, double* __restrict__ WP, double* __restrict__ xred) {
     const int f = lf[blockIdx.y];
     const FrontDev fr = fronts[f];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fr.F) return;
-    const int nch = (fr.nf + GC - 1) / GC;
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.F + r];
-    if (r < fr.nf) W[fr.woff + r] = s;                     // y
-    else WP[fr.woff + r] = WP[fr.woff + r] + s;            // u = w_B - G w_C
+    if (!BWD) {
+        if (r >= fr.F) return;
+        if (r < fr.nf) W[fr.woff + r] = stage_sum(ST_LINV, f, fr, r, sb);
+        else WP[fr.woff + r] += stage_sum(ST_L21, f, fr, r, sb);
+    } else {
+        if (r >= fr.nf) return;
+        xred[fr.red0 + r] = stage_sum(ST_UINV, f, fr, r, sb) + (fr.nb > 0 ? stage_sum(ST_U12, f, fr, r, sb) : 0.0);
+    }
 }
+template <int ST>
+__global__ void k_stage_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
+                               double* __restrict__ W, double* __restrict__ WP, double* __restrict__ xred) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    int br0, br1, bc0, bc1;
+    stage_block(ST, fr.nf, fr.F, br0, br1, bc0, bc1);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= br1 - br0) return;
+    const int r = br0 + q;
+    const double s = stage_sum(ST, f, fr, r, sb);
+    if (ST == ST_LINV) {
+        W[fr.woff + r] = s;
+        WP[fr.woff + r] = s;
+    } else if (ST == ST_L21) {
+        WP[fr.woff + r] += s;
+    } else if (ST == ST_U12) {
+        WP[fr.woff + r] += s;
+    } else {
+        xred[fr.red0 + r] = s;
+    }
+}
+
 // backward prologue: X = [y ; x_B]
 __global__ void k_bwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, const int* __restrict__ vars,
                              const double* __restrict__ W, const double* __restrict__ xred, double* __restrict__ WP) {
@@ -1023,19 +1095,6 @@ __global__ void k_bwd_gather(const FrontDev* __restrict__ fronts, const int* __r
     if (q >= fr.F) return;
     WP[fr.woff + q] = q < fr.nf ? W[fr.woff + q] : xred[vars[fr.voff + q]];
 }
-__global__ void k_bwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                             const double* __restrict__ part, const int64_t* __restrict__ part_off,
-                             double* __restrict__ xred) {
-    const int f = lf[blockIdx.y];
-    const FrontDev fr = fronts[f];
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fr.nf) return;
-    const int nch = (fr.F + GC - 1) / GC;
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += part[part_off[f] + int64_t(c) * fr.nf + r];
-    xred[fr.red0 + r] = s;
-}
-
 __global__ void k_fill(int n, double v, double* __restrict__ a) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) a[q] = v;
 }
@@ -1051,6 +1110,7 @@ int blocks_for(int64_t work, int per = NT) {
 // drivers
 // ===========================================================================
 NdLu::~NdLu() {
+    if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
     for (void* p : allocs) cudaFree(p);
 }
 
@@ -1121,66 +1181,165 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_cmax = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_npert = static_cast<int*>(dmalloc(lu, sizeof(int)));
     lu.d_wp = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
-    // solve-phase work items and partial-sum offsets
-    std::vector<WorkItem> fi, bi;
-    std::vector<int64_t> part_off(plan.nfronts, 0), part_off_b(plan.nfronts, 0);
-    int64_t poff = 0, poff_b = 0;
-    for (int f = 0; f < plan.nfronts; ++f) {
-        const FrontDev& fr = plan.fronts[f];
-        part_off[f] = poff;
-        poff += int64_t(fr.F) * ((fr.nf + GC - 1) / GC);
-        part_off_b[f] = poff_b;
-        poff_b += int64_t(fr.nf) * ((fr.F + GC - 1) / GC);
-    }
-    lu.fwd_items_start.clear();
-    lu.bwd_items_start.clear();
-    lu.fwd_bytes.assign(plan.nlevels, 0.0);
-    lu.bwd_bytes.assign(plan.nlevels, 0.0);
-    for (int h = 0; h < plan.nlevels; ++h) {
-        lu.fwd_items_start.push_back(int(fi.size()));
-        lu.bwd_items_start.push_back(int(bi.size()));
-        for (int f : plan.level_fronts[h]) {
+    // solve-phase partial-sum buffers (per stage) and work items (per launch
+    // group: G/H layout fuses LINV+L21 and UINV+U12; the L21/U12 layout runs
+    // the four stages as separate groups)
+    lu.gh = prec == 1;
+    std::vector<WorkItem> items[NSTAGE];
+    for (int st = 0; st < NSTAGE; ++st) {
+        std::vector<int64_t> off(plan.nfronts, 0);
+        int64_t poff = 0;
+        for (int f = 0; f < plan.nfronts; ++f) {
             const FrontDev& fr = plan.fronts[f];
-            const double nf = fr.nf, nb = fr.nb;
-            // forward: strict lower Linv11 + G (nb x nf); backward: upper Uinv11 + H (nf x nb)
-            lu.fwd_bytes[h] += double(ts) * (nf * (nf - 1) / 2 + nb * nf);
-            lu.bwd_bytes[h] += double(ts) * (nf * (nf + 1) / 2 + nf * nb);
-            // tiles that hold no entry of the triangular parts are skipped (their
-            // partial sums stay at the zero they are initialised to)
-            for (int c = 0; c * GC < fr.nf; ++c)
-                for (int r = 0; r * GR < fr.F; ++r)
-                    if (!(r * GR + GR <= fr.nf && c * GC >= r * GR + GR)) fi.push_back(WorkItem{f, r * GR, c * GC, c});
-            for (int c = 0; c * GC < fr.F; ++c)
-                for (int r = 0; r * GR < fr.nf; ++r)
-                    if (!(c * GC + GC <= r * GR)) bi.push_back(WorkItem{f, r * GR, c * GC, c});
+            int r0, r1, c0, c1;
+            stage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
+            off[f] = poff;
+            poff += int64_t(r1 - r0) * ((c1 - c0 + GC - 1) / GC);
         }
+        lu.d_stage_off[st] = upload(lu, off, s);
+        const size_t pb = sizeof(double) * size_t(std::max<int64_t>(poff, 1));
+        lu.d_stage_part[st] = static_cast<double*>(dmalloc(lu, pb));
+        ck(cudaMemsetAsync(lu.d_stage_part[st], 0, pb, s));
     }
-    lu.fwd_items_start.push_back(int(fi.size()));
-    lu.bwd_items_start.push_back(int(bi.size()));
-    lu.d_fwd_items = upload(lu, fi, s);
-    lu.d_bwd_items = upload(lu, bi, s);
-    lu.d_part_off = upload(lu, part_off, s);
-    lu.d_part = dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(poff, 1)));
-    ck(cudaMemsetAsync(lu.d_part, 0, sizeof(double) * size_t(std::max<int64_t>(poff, 1)), s));
-    lu.d_part_off_b = upload(lu, part_off_b, s);
-    lu.d_part_b = dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(poff_b, 1)));
-    ck(cudaMemsetAsync(lu.d_part_b, 0, sizeof(double) * size_t(std::max<int64_t>(poff_b, 1)), s));
-    // factorisation scratch (per level, per front)
-    std::vector<int64_t> sct, scg;
+    const int group_of[NSTAGE] = {0, 3, lu.gh ? 0 : 1, lu.gh ? 3 : 2};   // by stage
+    std::vector<WorkItem> gitems[4];
+    for (int g = 0; g < 4; ++g) {
+        lu.group_start[g].assign(1, 0);
+        lu.group_bytes[g].assign(plan.nlevels, 0.0);
+    }
+    for (int h = 0; h < plan.nlevels; ++h) {
+        for (int st = 0; st < NSTAGE; ++st) {
+            const int g = group_of[st];
+            for (int f : plan.level_fronts[h]) {
+                const FrontDev& fr = plan.fronts[f];
+                const double nf = fr.nf, nb = fr.nb;
+                lu.group_bytes[g][h] += double(ts) * (st == ST_LINV ? nf * (nf - 1) / 2
+                                                      : st == ST_UINV ? nf * (nf + 1) / 2 : nf * nb);
+                int r0, r1, c0, c1;
+                stage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
+                for (int c = c0, ch = 0; c < c1; c += GC, ++ch)
+                    for (int r = r0; r < r1; r += GR) {
+                        // tiles holding no entry of a triangular part are skipped
+                        if (st == ST_LINV && r + GR <= fr.nf && c >= r + GR) continue;
+                        if (st == ST_UINV && c + GC <= r) continue;
+                        gitems[g].push_back(WorkItem{f, r, c, ch, st});
+                    }
+            }
+        }
+        for (int g = 0; g < 4; ++g) lu.group_start[g].push_back(int(gitems[g].size()));
+    }
+    for (int g = 0; g < 4; ++g) lu.d_group_items[g] = upload(lu, gitems[g], s);
+    // factorisation scratch (per level, per front) for G/H
+    std::vector<int64_t> scg;
     int64_t mx = 0;
     for (int h = 0; h < plan.nlevels; ++h) {
-        int64_t a = 0, b = 0;
+        int64_t b = 0;
         for (int f : plan.level_fronts[h]) {
             const FrontDev& fr = plan.fronts[f];
-            sct.push_back(a);
-            a += int64_t(plan.panel) * fr.nf;
             scg.push_back(b);
-            b += int64_t(fr.nf) * fr.nb;
+            if (lu.gh) b += int64_t(fr.nf) * fr.nb;
         }
-        mx = std::max(mx, std::max(a, b));
+        mx = std::max(mx, b);
     }
-    lu.d_sc_tr = upload(lu, sct, s);
     lu.d_sc_gh = upload(lu, scg, s);
+    // recursive triangular inversion: tasks and 64x64 tiles per (level, merge
+    // size, phase); phase-1 products go to a scratch area of their own
+    {
+        std::vector<TriTask> tasks;
+        std::vector<TriTile> tiles;
+        int64_t tmax = 0;
+        lu.tri_ranges.clear();
+        for (int h = 0; h < plan.nlevels; ++h) {
+            std::vector<std::pair<int, int>> lv;
+            auto emit = [&](const TriTask& t) {
+                const int id = int(tasks.size());
+                tasks.push_back(t);
+                for (int j = 0; j < t.N; j += 64)
+                    for (int i = 0; i < t.M; i += 64) tiles.push_back(TriTile{id, i, j});
+            };
+            // (1) merges inside the 256-row super-blocks: sz = 32, 64, 128
+            for (int sz = plan.panel; sz < TRI_SB && sz < plan.level_maxnf[h]; sz *= 2) {
+                for (int phase = 0; phase < 2; ++phase) {
+                    const int tb = int(tiles.size());
+                    int64_t toff = 0;
+                    for (int f : plan.level_fronts[h]) {
+                        const FrontDev& fr = plan.fronts[f];
+                        const int nf = fr.nf, F = fr.F;
+                        for (int a0 = 0; a0 + sz < nf; a0 += 2 * sz) {
+                            const int a1 = a0 + sz, d0 = a1, d1 = std::min(nf, a1 + sz);
+                            const int na = a1 - a0, nd = d1 - d0;
+                            for (int up = 0; up < 2; ++up) {
+                                const int64_t tcur = toff;
+                                toff += int64_t(na) * nd;
+                                if (!up && phase == 0)            // T = L21blk * Ainv   (nd x na)
+                                    emit(TriTask{fr.off + int64_t(a0) * F + d0, fr.off + int64_t(a0) * F + a0, tcur,
+                                                 F, F, nd, nd, na, na, OP_DENSE, OP_LOWER_UNIT, 0, 0, 1, 1.f});
+                                else if (!up)                     // X21 = -Dinv * T
+                                    emit(TriTask{fr.off + int64_t(d0) * F + d0, tcur, fr.off + int64_t(a0) * F + d0,
+                                                 F, nd, F, nd, na, nd, OP_LOWER_UNIT, OP_DENSE, 0, 1, 0, -1.f});
+                                else if (phase == 0)              // T = Ainv * U12blk   (na x nd)
+                                    emit(TriTask{fr.off + int64_t(a0) * F + a0, fr.off + int64_t(d0) * F + a0, tcur,
+                                                 F, F, na, na, nd, na, OP_UPPER, OP_DENSE, 0, 0, 1, 1.f});
+                                else                              // X12 = -T * Dinv
+                                    emit(TriTask{tcur, fr.off + int64_t(d0) * F + d0, fr.off + int64_t(d0) * F + a0,
+                                                 na, F, F, na, nd, nd, OP_DENSE, OP_UPPER, 1, 0, 0, -1.f});
+                            }
+                        }
+                    }
+                    tmax = std::max(tmax, toff);
+                    lv.push_back({tb, int(tiles.size())});
+                }
+            }
+            // (2) block-row steps over the super-blocks (row-oriented inversion,
+            //     whose rounding involves one large inverse per product):
+            //     lower, top down:  X[Ri, 0:i0] = -Linv_ii (L[Ri, 0:i0] X[0:i0, 0:i0])
+            //     upper, bottom up: Y[Ri, i1:nf] = -Uinv_ii (U[Ri, i1:nf] Y[i1:nf, i1:nf])
+            const int nsb_max = (plan.level_maxnf[h] + TRI_SB - 1) / TRI_SB;
+            for (int t = 1; t < nsb_max; ++t) {
+                for (int phase = 0; phase < 2; ++phase) {
+                    const int tb = int(tiles.size());
+                    int64_t toff = 0;
+                    for (int f : plan.level_fronts[h]) {
+                        const FrontDev& fr = plan.fronts[f];
+                        const int nf = fr.nf, F = fr.F;
+                        const int nsb = (nf + TRI_SB - 1) / TRI_SB;
+                        if (t >= nsb) continue;
+                        {   // lower, super-block row i = t
+                            const int r0 = t * TRI_SB, r1 = std::min(nf, r0 + TRI_SB), m = r1 - r0, w = r0;
+                            const int64_t tcur = toff;
+                            toff += int64_t(m) * w;
+                            if (phase == 0)   // T = L[Ri, 0:r0] * X[0:r0, 0:r0]   (m x w)
+                                emit(TriTask{fr.off + r0, fr.off, tcur, F, F, m, m, w, w, OP_DENSE, OP_LOWER_UNIT,
+                                             0, 0, 1, 1.f});
+                            else              // X[Ri, 0:r0] = -Linv_ii * T
+                                emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + r0, F, m, F, m, w, m,
+                                             OP_LOWER_UNIT, OP_DENSE, 0, 1, 0, -1.f});
+                        }
+                        {   // upper, super-block row i = nsb - 1 - t
+                            const int i = nsb - 1 - t;
+                            const int r0 = i * TRI_SB, r1 = r0 + TRI_SB, m = r1 - r0, w = nf - r1;
+                            const int64_t tcur = toff;
+                            toff += int64_t(m) * w;
+                            if (phase == 0)   // T = U[Ri, r1:nf] * Y[r1:nf, r1:nf]   (m x w)
+                                emit(TriTask{fr.off + int64_t(r1) * F + r0, fr.off + int64_t(r1) * F + r1, tcur,
+                                             F, F, m, m, w, w, OP_DENSE, OP_UPPER, 0, 0, 1, 1.f});
+                            else              // Y[Ri, r1:nf] = -Uinv_ii * T
+                                emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + int64_t(r1) * F + r0,
+                                             F, m, F, m, w, m, OP_UPPER, OP_DENSE, 0, 1, 0, -1.f});
+                        }
+                    }
+                    tmax = std::max(tmax, toff);
+                    lv.push_back({tb, int(tiles.size())});
+                }
+            }
+            lu.tri_ranges.push_back(lv);
+        }
+        lu.d_tri_tasks = upload(lu, tasks, s);
+        lu.d_tri_tiles = upload(lu, tiles, s);
+        lu.d_tri_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax, 1)));
+        lu.tri_flops = 0.0;
+        for (const TriTask& t : tasks) lu.tri_flops += double(t.M) * t.N * t.K;   // ~ half are structural zeros
+    }
     lu.d_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(mx, 1)));
     ck(cudaStreamSynchronize(s));
 }
@@ -1255,31 +1414,28 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
         }
         // explicit inverses for the solve phase
         const int maxblk = (maxnf + B - 1) / B;
-        const int64_t* sct = lu.d_sc_tr + lu.level_start[h];
-        const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
         cudaEvent_t ev_inv = lu.timer ? lu.timer->start(s) : nullptr;
         k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
-        const int ctiles = (maxnf + 63) / 64;
-        const int cblocks = blocks_for(int64_t(maxnf) * B);
-        for (int i = 1; i < maxblk; ++i) {
-            k_trinv_step<T, B, false><<<dim3(ctiles, nfr), 256, 0, s>>>(lu.d_fronts, lf, i, front, dinv, scratch, sct); IEMIC_COUNT_LAUNCH();
-            k_trinv_copy<T, B, false><<<dim3(cblocks, nfr), NT, 0, s>>>(lu.d_fronts, lf, i, front, scratch, sct); IEMIC_COUNT_LAUNCH();
+        for (const auto& rg : lu.tri_ranges[h]) {
+            if (rg.second > rg.first)
+                k_tri_gemm<T><<<rg.second - rg.first, 256, 0, s>>>(
+                    static_cast<const TriTask*>(lu.d_tri_tasks), static_cast<const TriTile*>(lu.d_tri_tiles) + rg.first,
+                    front, static_cast<T*>(lu.d_tri_scratch)); IEMIC_COUNT_LAUNCH();
         }
-        for (int i = maxblk - 2; i >= 0; --i) {
-            k_trinv_step<T, B, true><<<dim3(ctiles, nfr), 256, 0, s>>>(lu.d_fronts, lf, i, front, dinv, scratch, sct); IEMIC_COUNT_LAUNCH();
-            k_trinv_copy<T, B, true><<<dim3(cblocks, nfr), NT, 0, s>>>(lu.d_fronts, lf, i, front, scratch, sct); IEMIC_COUNT_LAUNCH();
-        }
-        int64_t mt = 0, mnb = 0;
-        for (int f : P.level_fronts[h]) {
-            const FrontDev& fr = P.fronts[f];
-            mt = std::max<int64_t>(mt, int64_t((fr.nf + 63) / 64) * ((fr.nb + 63) / 64));
-            mnb = std::max<int64_t>(mnb, int64_t(fr.nf) * fr.nb);
-        }
-        if (mt > 0) {
-            k_gh<T, false><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-            k_gh_copy<T, false><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-            k_gh<T, true><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-            k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+        if (lu.gh) {
+            const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
+            int64_t mt = 0, mnb = 0;
+            for (int f : P.level_fronts[h]) {
+                const FrontDev& fr = P.fronts[f];
+                mt = std::max<int64_t>(mt, int64_t((fr.nf + 63) / 64) * ((fr.nb + 63) / 64));
+                mnb = std::max<int64_t>(mnb, int64_t(fr.nf) * fr.nb);
+            }
+            if (mt > 0) {
+                k_gh<T, false><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+                k_gh_copy<T, false><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+                k_gh<T, true><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+                k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+            }
         }
         if (ev_inv) lu.timer->stop(ev_inv, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
     }
@@ -1293,67 +1449,128 @@ void ndlu_factor(NdLu& lu, const int* rp, const int* ci, const double* values, c
     else factor_t<double, 32>(lu, rp, ci, values, s);
 }
 
-template <class T, int B, class TV>
-static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, const TV* r, TV* z, cudaStream_t s) {
+static StageBufs stage_bufs(NdLu& lu) {
+    StageBufs sb;
+    for (int st = 0; st < NSTAGE; ++st) {
+        sb.part[st] = lu.d_stage_part[st];
+        sb.off[st] = lu.d_stage_off[st];
+    }
+    return sb;
+}
+template <class T>
+static void launch_group(NdLu& lu, int g, int h, const T* front, double* WP, cudaStream_t s) {
+    const int ni = lu.group_start[g][h + 1] - lu.group_start[g][h];
+    if (!ni) return;
+    cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
+    k_gemv_part<T><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_group_items[g]) +
+                                         lu.group_start[g][h], front, WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
+    if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.group_bytes[g][h], 2.0 * lu.group_bytes[g][h] / sizeof(T));
+}
+template <int ST>
+static void launch_reduce(NdLu& lu, int h, double* W, double* WP, double* red, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+    const int* lf = lu.d_level_fronts + lu.level_start[h];
+    const int rows = ST == ST_L21 ? P.level_maxF[h] : P.level_maxnf[h];
+    if (rows <= 0) return;
+    KTimer* kt = lu.timer;
+    cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+    k_stage_reduce<ST><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red); IEMIC_COUNT_LAUNCH();
+    if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+}
+template <bool BWD>
+static void launch_fused_reduce(NdLu& lu, int h, double* W, double* WP, double* red, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+    const int* lf = lu.d_level_fronts + lu.level_start[h];
+    const int rows = BWD ? P.level_maxnf[h] : P.level_maxF[h];
+    if (rows <= 0) return;
+    KTimer* kt = lu.timer;
+    cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+    k_fused_reduce<BWD><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red); IEMIC_COUNT_LAUNCH();
+    if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+}
+
+// The forward and backward sweeps over the levels: internal buffers only
+// (red -> red), so they can be captured once into a CUDA graph.
+template <class T, int B>
+static void sweeps_t(NdLu& lu, cudaStream_t s) {
     const NdPlan& P = *lu.plan;
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
     double* WP = static_cast<double*>(lu.d_wp);
-    double* part = static_cast<double*>(lu.d_part);
-    double* part_b = static_cast<double*>(lu.d_part_b);
     const T* front = static_cast<const T*>(lu.d_front);
     KTimer* kt = lu.timer;
-    cudaEvent_t ev_so = kt ? kt->start(s) : nullptr;
-    k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
-    if (ev_so) kt->stop(ev_so, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         {
-            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            cudaEvent_t ev = kt ? kt->start(s) : nullptr;
             k_fwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
-            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+            if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        const int ni = lu.fwd_items_start[h + 1] - lu.fwd_items_start[h];
-        cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
-        if (ni) {
-            k_gemv_part<T, false><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_fwd_items) +
-                                                        lu.fwd_items_start[h], front, WP, part, lu.d_part_off); IEMIC_COUNT_LAUNCH();
-        }
-        if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.fwd_bytes[h], 2.0 * lu.fwd_bytes[h] / sizeof(T));
-        {
-            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
-            k_fwd_reduce<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part, lu.d_part_off, W,
-                                                                                    WP); IEMIC_COUNT_LAUNCH();
-            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        if (lu.gh) {
+            launch_group<T>(lu, 0, h, front, WP, s);
+            launch_fused_reduce<false>(lu, h, W, WP, red, s);
+        } else {
+            launch_group<T>(lu, 0, h, front, WP, s);
+            launch_reduce<ST_LINV>(lu, h, W, WP, red, s);
+            launch_group<T>(lu, 1, h, front, WP, s);
+            launch_reduce<ST_L21>(lu, h, W, WP, red, s);
         }
     }
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         {
-            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+            cudaEvent_t ev = kt ? kt->start(s) : nullptr;
             k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
-            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+            if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        const int ni = lu.bwd_items_start[h + 1] - lu.bwd_items_start[h];
-        cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
-        if (ni) {
-            k_gemv_part<T, true><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_bwd_items) +
-                                                       lu.bwd_items_start[h], front, WP, part_b, lu.d_part_off_b); IEMIC_COUNT_LAUNCH();
-        }
-        if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.bwd_bytes[h], 2.0 * lu.bwd_bytes[h] / sizeof(T));
-        {
-            cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
-            k_bwd_reduce<<<dim3((P.level_maxnf[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, part_b, lu.d_part_off_b,
-                                                                                     red); IEMIC_COUNT_LAUNCH();
-            if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        if (lu.gh) {
+            launch_group<T>(lu, 3, h, front, WP, s);
+            launch_fused_reduce<true>(lu, h, W, WP, red, s);
+        } else {
+            launch_group<T>(lu, 2, h, front, WP, s);
+            launch_reduce<ST_U12>(lu, h, W, WP, red, s);
+            launch_group<T>(lu, 3, h, front, WP, s);
+            launch_reduce<ST_UINV>(lu, h, W, WP, red, s);
         }
     }
+}
+
+template <class T, int B, class TV>
+static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, const TV* r, TV* z, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    double* red = static_cast<double*>(lu.d_red);
+    KTimer* kt = lu.timer;
     {
-        cudaEvent_t ev_o = kt ? kt->start(s) : nullptr;
+        cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+        k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
+        if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+    }
+    if (kt && kt->on) {
+        sweeps_t<T, B>(lu, s);   // eager, so every launch can be timed
+    } else {
+        if (!lu.sweep_exec) {
+            cudaGraph_t g = nullptr;
+            ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const long long n0 = launch_counter();
+            sweeps_t<T, B>(lu, s);
+            lu.sweep_launches = launch_counter() - n0;
+            launch_counter() = n0;
+            ck(cudaStreamEndCapture(s, &g));
+            const cudaError_t e = cudaGraphInstantiate(&lu.sweep_exec, g, 0);
+            cudaGraphDestroy(g);
+            ck(e);
+        }
+        ck(cudaGraphLaunch(lu.sweep_exec, s));
+        launch_counter() += lu.sweep_launches;
+    }
+    {
+        cudaEvent_t ev = kt ? kt->start(s) : nullptr;
         k_expand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dc, red, r, z); IEMIC_COUNT_LAUNCH();
-        if (ev_o) kt->stop(ev_o, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
     ck(cudaGetLastError());
 }

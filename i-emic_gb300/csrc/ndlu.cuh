@@ -52,7 +52,6 @@ struct NdLu {
     int prec = 0;   // 0 FP64, 1 FP32
     const NdPlan* plan = nullptr;
     KTimer* timer = nullptr;                // optional launch timing (owned by the engine)
-    std::vector<double> fwd_bytes, bwd_bytes;   // per level: factor bytes one GEMV sweep reads
     // device copies of the plan
     FrontDev* d_fronts = nullptr;
     int* d_level_fronts = nullptr;          // concatenated per level
@@ -72,14 +71,23 @@ struct NdLu {
     void* d_red = nullptr;                  // reduced rhs / solution (T)
     int* d_npert = nullptr;                 // perturbed-pivot counter
     void* d_wp = nullptr;                   // permuted / gathered solve vectors (FP64)
-    void* d_part = nullptr;                 // forward GEMV partial sums (FP64), F x chunks per front
-    int64_t* d_part_off = nullptr;
-    void* d_part_b = nullptr;               // backward GEMV partial sums (FP64), nf x chunks per front
-    int64_t* d_part_off_b = nullptr;
-    void *d_fwd_items = nullptr, *d_bwd_items = nullptr;   // GEMV work items per level
-    std::vector<int> fwd_items_start, bwd_items_start;
-    int64_t *d_sc_tr = nullptr, *d_sc_gh = nullptr;         // scratch offsets per front (by level)
+    // solve phase: partial-sum buffers and per-front offsets per GEMV stage
+    // (Linv11, Uinv11, L21 or G, U12 or H), work items per launch group
+    bool gh = false;                        // fronts hold G/H (FP32) instead of L21/U12 (FP64)
+    double* d_stage_part[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t* d_stage_off[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* d_group_items[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<int> group_start[4];        // per level offsets into d_group_items
+    std::vector<double> group_bytes[4];     // per level: factor bytes the group reads
+    int64_t* d_sc_gh = nullptr;             // G/H scratch offsets per front (by level)
+    // recursive triangular inversion: tasks, tiles, per level the tile ranges
+    // of its launches, and the scratch of the first product of each merge
+    void *d_tri_tasks = nullptr, *d_tri_tiles = nullptr, *d_tri_scratch = nullptr;
+    std::vector<std::vector<std::pair<int, int>>> tri_ranges;
+    double tri_flops = 0.0;
     void* d_scratch = nullptr;
+    cudaGraphExec_t sweep_exec = nullptr; // captured forward + backward level sweeps
+    long long sweep_launches = 0;           // kernels in the captured sweeps
     int npert = 0;
     bool factored = false;
     std::vector<void*> allocs;
