@@ -60,6 +60,10 @@ struct Engine {
     NdLu* lu32 = nullptr;
     Krylov* kry = nullptr;
     std::vector<int> h_col;   // host copy of the CSR column indices
+    // transposed Jacobian for adjoint solves: pattern, slot map, values
+    int *d_rowT = nullptr, *d_colT = nullptr, *d_permT = nullptr;
+    double* d_valT = nullptr;
+    bool jacT_stale = true;
     KTimer timer;             // optional per-kernel-class device timing
 
     ~Engine();
@@ -82,6 +86,7 @@ struct Engine {
     void build_preconditioner(int precision);
     int solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);
     int solve_transpose_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);
+    void ensure_transpose();
     void apply_precon(int precision, const double* v, double* out);
     NdLu*& lu_for(int precision);
     const std::vector<int>& host_col_idx();

@@ -288,12 +288,24 @@ void Engine::apply_precon(int precision, const double* v, double* out) {
     ck(cudaGetLastError());
 }
 
+// M^{-1} v (or M^{-T} v for the adjoint) in the Krylov precision T
+template <class T>
+static void precond(NdLu& lu, Engine& e, const T* v, T* z, bool transpose, cudaStream_t s) {
+    if constexpr (sizeof(T) == 8) {
+        if (transpose) {
+            ndlu_apply_transpose(lu, v, z, s);
+            return;
+        }
+    }
+    ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, v, z, sizeof(T) == 4, s);
+}
+
 // One restarted-GMRES solve of J x = b in precision T, x0 = 0, right
 // preconditioned by the factorisation `lu`. `b` must not alias the Krylov
 // workspace. Returns the inner iterations used.
 template <class T>
-static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, int maxit, double tol,
-                 double* relres_out) {
+static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* vals, const T* b, T* x, int m, int maxit,
+                 double tol, double* relres_out, bool transpose = false) {
     Krylov& K = *e.kry;
     const int n = e.ndim;
     cudaStream_t s = e.stream;
@@ -326,7 +338,7 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
         if (first) {
             ck(cudaMemcpyAsync(w, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
         } else {
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, x, z); IEMIC_COUNT_LAUNCH();
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, x, z); IEMIC_COUNT_LAUNCH();
             sub_from<T><<<G, 256, 0, s>>>(n, b, z, w); IEMIC_COUNT_LAUNCH();
         }
         first = false;
@@ -339,9 +351,9 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
         g[0] = beta;
         int j = 0;
         for (; j < m && it < maxit;) {
-            ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, V + size_t(j) * n, z, sizeof(T) == 4, s);
+            precond(lu, e, V + size_t(j) * n, z, transpose, s);
             cudaEvent_t ev = e.timer.start(s);
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, e.d_rowptr, e.d_col, vals, z, w); IEMIC_COUNT_LAUNCH();
+            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, z, w); IEMIC_COUNT_LAUNCH();
             e.timer.stop(ev, s, IEMIC_KC_SPMV, spmv_bytes, 2.0 * double(e.nnz));
             for (int pass = 0; pass < 2; ++pass) {   // CGS2
                 multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
@@ -385,7 +397,7 @@ static int gmres(Engine& e, NdLu& lu, const T* vals, const T* b, T* x, int m, in
         }
         ck(cudaMemcpyAsync(K.y, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         combine<T><<<G, 256, 0, s>>>(n, j, V, K.y, w); IEMIC_COUNT_LAUNCH();
-        ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, w, z, sizeof(T) == 4, s);
+        precond(lu, e, w, z, transpose, s);
         add_to<T><<<G, 256, 0, s>>>(n, z, x); IEMIC_COUNT_LAUNCH();
         ck(cudaStreamSynchronize(s));   // y is a host temporary
     }
@@ -435,7 +447,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     if (!fp32_krylov) {
         scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
         double est = 1.0;
-        st.iters += gmres<double>(*this, *lu, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est);
+        st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est);
         axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
         residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
         multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
@@ -458,7 +470,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
             convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm); IEMIC_COUNT_LAUNCH();
             double est = 1.0;
             double inner = std::max(o.inner_tol, 0.5 * o.tol / relres);
-            st.iters += gmres<float>(*this, *lu, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner, &est);
+            st.iters += gmres<float>(*this, *lu, d_rowptr, d_col, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner, &est);
             axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x); IEMIC_COUNT_LAUNCH();
             residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
             multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
@@ -478,8 +490,92 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     return rc;
 }
 
-int Engine::solve_transpose_dev(const double*, double*, const iemic_solve_opts&, iemic_solve_stats&) {
-    return IEMIC_ERR_STATE;
+// J^T values in the transposed pattern (refreshed when J changed)
+__global__ void k_gather_vals(int64_t nnz, const int* __restrict__ perm, const double* __restrict__ v,
+                              double* __restrict__ vt) {
+    for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < nnz; q += int64_t(gridDim.x) * blockDim.x)
+        vt[q] = v[perm[q]];
+}
+
+void Engine::ensure_transpose() {
+    if (!d_rowT) {
+        const std::vector<int>& ci = host_col_idx();
+        std::vector<int> rt(static_cast<size_t>(ndim) + 1, 0), ct(static_cast<size_t>(nnz)), pm(static_cast<size_t>(nnz));
+        for (int64_t q = 0; q < nnz; ++q) rt[size_t(ci[q]) + 1] += 1;
+        for (int r = 0; r < ndim; ++r) rt[r + 1] += rt[r];
+        std::vector<int> fill(rt.begin(), rt.end() - 1);
+        for (int r = 0; r < ndim; ++r)
+            for (int q = row_ptr[r]; q < row_ptr[r + 1]; ++q) {
+                const int d = fill[ci[q]]++;
+                ct[d] = r;
+                pm[d] = q;
+            }
+        d_rowT = static_cast<int*>(dalloc(sizeof(int) * rt.size()));
+        d_colT = static_cast<int*>(dalloc(sizeof(int) * ct.size()));
+        d_permT = static_cast<int*>(dalloc(sizeof(int) * pm.size()));
+        d_valT = static_cast<double*>(dalloc(sizeof(double) * size_t(nnz)));
+        ck(cudaMemcpyAsync(d_rowT, rt.data(), sizeof(int) * rt.size(), cudaMemcpyHostToDevice, stream));
+        ck(cudaMemcpyAsync(d_colT, ct.data(), sizeof(int) * ct.size(), cudaMemcpyHostToDevice, stream));
+        ck(cudaMemcpyAsync(d_permT, pm.data(), sizeof(int) * pm.size(), cudaMemcpyHostToDevice, stream));
+        ck(cudaStreamSynchronize(stream));
+        jacT_stale = true;
+    }
+    if (jacT_stale) {
+        k_gather_vals<<<vgrid(int(std::min<int64_t>(nnz, 1 << 30))), 256, 0, stream>>>(nnz, d_permT, d_val, d_valT); IEMIC_COUNT_LAUNCH();
+        ck(cudaGetLastError());
+        jacT_stale = false;
+    }
+}
+
+// Adjoint solve J^T x = b: FP64 GMRES on J^T, right preconditioned by M^{-T}
+// from the same factorisation as the forward solve (FP64 or FP32 factors).
+int Engine::solve_transpose_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
+    if (!jac_valid) return IEMIC_ERR_STATE;
+    if (o.precision == IEMIC_PREC_FP32_KRYLOV) return IEMIC_ERR_ARG;
+    const int prec = o.precision == IEMIC_PREC_FP64 ? IEMIC_PREC_FP64 : IEMIC_PREC_MIXED;
+    auto t0 = std::chrono::steady_clock::now();
+    ensure_solver();
+    NdLu*& lu = lu_for(prec);
+    const bool stale = prec == IEMIC_PREC_MIXED ? fact32_stale : fact64_stale;
+    if (!lu || !lu->factored || (stale && !o.reuse_preconditioner)) {
+        build_preconditioner(prec);
+        st.factorizations += 1;
+    }
+    st.perturbed_pivots = lu->npert;
+    ensure_transpose();
+    auto t1 = std::chrono::steady_clock::now();
+    st.time_factor_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    ensure_krylov(*this, o.restart, 0);
+    Krylov& K = *kry;
+    const int n = ndim, G = vgrid(n);
+    cudaStream_t s = stream;
+    multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    double bn2 = 0.0;
+    ck(cudaMemcpyAsync(&bn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    const double bnorm = std::sqrt(bn2);
+    if (!std::isfinite(bnorm)) return IEMIC_ERR_NAN;
+    ck(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    if (bnorm == 0.0) {
+        st.relres = 0.0;
+        return IEMIC_OK;
+    }
+    scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
+    double est = 1.0;
+    st.iters += gmres<double>(*this, *lu, d_rowT, d_colT, d_valT, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est,
+                              true);
+    axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
+    residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowT, d_colT, d_valT, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+    multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    double rn2 = 0.0;
+    ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    st.relres = std::sqrt(rn2) / bnorm;
+    timer.drain();
+    st.time_solve_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+    return st.relres <= o.tol ? IEMIC_OK : IEMIC_ERR_NOT_CONVERGED;
 }
 
 }  // namespace iemic

@@ -1095,6 +1095,200 @@ __global__ void k_bwd_gather(const FrontDev* __restrict__ fronts, const int* __r
     if (q >= fr.F) return;
     WP[fr.woff + q] = q < fr.nf ? W[fr.woff + q] : xred[vars[fr.voff + q]];
 }
+// ---------------------------------------------------------------------------
+// transposed solve phase (A^T y = c with the same factors; A = P^T L U per
+// front):
+//   leaves -> root: v_o = Uinv11^T c_o;  u_B = c_B - U12^T v_o  (G/H: - H^T c_o)
+//   root -> leaves: t = v_o - L21^T y_B; y_o = P^T Linv11^T t  (G/H: P^T (Linv11^T v_o - G^T y_B))
+// Each stage reads one stored block column-wise: a warp owns a column, its
+// lanes stride down the rows (coalesced), and a tile of 64 columns x 256 rows
+// writes one partial sum per column.
+// ---------------------------------------------------------------------------
+constexpr int TCOLS = 64, TROWS = 256;
+enum { TS_UINV = 0, TS_U12 = 1, TS_LINV = 2, TS_L21 = 3 };
+// rows summed over and columns produced by a transposed stage
+__host__ __device__ inline void tstage_block(int st, int nf, int F, int& r0, int& r1, int& c0, int& c1) {
+    r0 = st == TS_L21 ? nf : 0;
+    r1 = st == TS_L21 ? F : nf;
+    c0 = st == TS_U12 ? nf : 0;
+    c1 = st == TS_U12 ? F : nf;
+}
+struct TStageBufs {
+    double* part[4];
+    const int64_t* off[4];
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+template <class T, int ST>
+__device__ __forceinline__ void tgemv_stage(const WorkItem& it, const FrontDev& fr, const T* __restrict__ front,
+                                            const double* __restrict__ X, const TStageBufs& sb) {
+    const int F = fr.F, nf = fr.nf;
+    int br0, br1, bc0, bc1;
+    tstage_block(ST, nf, F, br0, br1, bc0, bc1);
+    __shared__ double txs[TROWS];
+    __shared__ float2 txs2[TROWS];
+    const double* x = X + fr.woff;
+    for (int q = threadIdx.x; q < TROWS; q += blockDim.x) {
+        const int r = it.row0 + q;
+        const double v = r < br1 ? x[r] : 0.0;
+        if (sizeof(T) == 4) {
+            const float h = __double2float_rn(v);
+            txs2[q] = make_float2(h, __double2float_rn(v - double(h)));
+        } else {
+            txs[q] = v;
+        }
+    }
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int rend = min(br1, it.row0 + TROWS);
+    for (int cc = warp; cc < TCOLS; cc += blockDim.x / 32) {
+        const int c = it.col0 + cc;
+        if (c >= bc1) break;
+        const T* col = front + fr.off + int64_t(c) * F;
+        // rows of this column that the stage uses
+        int rb = it.row0, re = rend;
+        if (ST == TS_UINV) re = min(re, c + 1);          // upper incl. diagonal: r <= c
+        if (ST == TS_LINV) rb = max(rb, c + 1);          // strict lower: r > c
+        double out;
+        if (sizeof(T) == 4) {
+            float sh = 0.f, sl = 0.f;
+            for (int r = rb + lane; r < re; r += 32) {
+                const float2 xv = txs2[r - it.row0];
+                dd_acc(sh, sl, float(col[r]), xv.x, xv.y);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, sh, o), ol = __shfl_xor_sync(0xffffffffu, sl, o);
+                float t, e;
+                two_sum(sh, oh, t, e);
+                sh = t;
+                sl = __fadd_rn(__fadd_rn(sl, ol), e);
+            }
+            out = double(sh) + double(sl);
+        } else {
+            double acc = 0.0;
+            for (int r = rb + lane; r < re; r += 32) acc += double(col[r]) * txs[r - it.row0];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            out = acc;
+        }
+        if (ST == TS_LINV && c >= it.row0 && c < rend)   // unit diagonal
+            out += sizeof(T) == 4 ? txs2[c - it.row0].x + double(txs2[c - it.row0].y) : txs[c - it.row0];
+        if (ST == TS_U12 || ST == TS_L21) out = -out;
+        if (lane == 0) sb.part[ST][sb.off[ST][it.front] + int64_t(it.chunk) * (bc1 - bc0) + (c - bc0)] = out;
+    }
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_tgemv_part(const FrontDev* __restrict__ fronts,
+                                                    const WorkItem* __restrict__ items, const T* __restrict__ front,
+                                                    const double* __restrict__ X, TStageBufs sb) {
+    const WorkItem it = items[blockIdx.x];
+    const FrontDev fr = fronts[it.front];
+    switch (it.stage) {
+        case TS_UINV: tgemv_stage<T, TS_UINV>(it, fr, front, X, sb); break;
+        case TS_U12: tgemv_stage<T, TS_U12>(it, fr, front, X, sb); break;
+        case TS_LINV: tgemv_stage<T, TS_LINV>(it, fr, front, X, sb); break;
+        default: tgemv_stage<T, TS_L21>(it, fr, front, X, sb); break;
+    }
+}
+__device__ __forceinline__ double tstage_sum(int st, int f, const FrontDev& fr, int c, const TStageBufs& sb) {
+    int br0, br1, bc0, bc1;
+    tstage_block(st, fr.nf, fr.F, br0, br1, bc0, bc1);
+    const int cols = bc1 - bc0, nch = (br1 - br0 + TROWS - 1) / TROWS;
+    const double* p = sb.part[st] + sb.off[st][f] + (c - bc0);
+    double s = 0.0;
+    for (int q = 0; q < nch; ++q) s += p[int64_t(q) * cols];
+    return s;
+}
+// leaves -> root prologue: W = [c_own ; 0] + children's update vectors (no permutation)
+__global__ void __launch_bounds__(NT) k_tfwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                                    const int* __restrict__ child_of, const int* __restrict__ emap,
+                                                    const double* __restrict__ red, double* __restrict__ W,
+                                                    double* __restrict__ WP) {
+    const int f = lf[blockIdx.x];
+    const FrontDev fr = fronts[f];
+    const int F = fr.F, nf = fr.nf, tid = threadIdx.x;
+    double* w = WP + fr.woff;
+    for (int q = tid; q < F; q += NT) w[q] = q < nf ? red[fr.red0 + q] : 0.0;
+    __syncthreads();
+    for (int s = 0; s < 2; ++s) {
+        const int c = child_of[2 * f + s];
+        if (c < 0) continue;
+        const FrontDev ch = fronts[c];
+        const double* u = W + ch.woff + ch.nf;   // child's update vector (kept in W)
+        const int* em = emap + ch.emap_off;
+        for (int a = tid; a < ch.nb; a += NT) w[em[a]] += u[a];
+        __syncthreads();
+    }
+}
+// leaves -> root epilogues. Two-stage: (UINV) v -> W[own], WP[own]; (U12)
+// W[B] = c_B + sums. Fused (H): both from the same launch.
+template <int MODE>   // 0: UINV only, 1: U12 only, 2: both (fused)
+__global__ void k_tfwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, TStageBufs sb,
+                              double* __restrict__ W, double* __restrict__ WP) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.F) return;
+    if (q < fr.nf) {
+        if (MODE != 1) {
+            const double v = tstage_sum(TS_UINV, f, fr, q, sb);
+            W[fr.woff + q] = v;
+            WP[fr.woff + q] = v;
+        }
+    } else if (MODE != 0) {
+        W[fr.woff + q] = WP[fr.woff + q] + tstage_sum(TS_U12, f, fr, q, sb);
+    }
+}
+// root -> leaves prologue: WP = [v_own ; y_B]
+__global__ void k_tbwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                              const int* __restrict__ vars, const double* __restrict__ W,
+                              const double* __restrict__ yred, double* __restrict__ WP) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.F) return;
+    WP[fr.woff + q] = q < fr.nf ? W[fr.woff + q] : yred[vars[fr.voff + q]];
+}
+// root -> leaves epilogues. MODE 0 (two-stage, after L21^T): WP[own] = v + sum;
+// MODE 1 (after LINV^T, or fused LINV^T + G^T): y_o = P^T (sum) scattered to yred
+template <int MODE>
+__global__ void k_tbwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, TStageBufs sb,
+                              const int* __restrict__ piv, double* __restrict__ WP, double* __restrict__ yred,
+                              int fused, int B) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.nf) return;
+    if (MODE == 0) {
+        WP[fr.woff + q] += tstage_sum(TS_L21, f, fr, q, sb);
+    } else {
+        double y = tstage_sum(TS_LINV, f, fr, q, sb);
+        if (fused && fr.nb > 0) y += tstage_sum(TS_L21, f, fr, q, sb);
+        const int p = (q / B) * B;
+        yred[fr.red0 + p + piv[fr.red0 + q]] = y;
+    }
+}
+// reduced transposed right-hand side: column-scaled wet entries
+template <class TV>
+__global__ void k_treduce_rhs(int nred, const int* __restrict__ r2g, const double* __restrict__ dc,
+                              const TV* __restrict__ r, double* __restrict__ red) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nred; q += gridDim.x * blockDim.x) {
+        const int g = r2g[q];
+        red[q] = dc[g] * double(r[g]);
+    }
+}
+// transposed expansion: row-scaled solution, identity unknowns pass r, gauge zero
+template <class TV>
+__global__ void k_texpand(int ndim, const int* __restrict__ g2r, const char* __restrict__ isdry,
+                          const double* __restrict__ dr, const double* __restrict__ red, const TV* __restrict__ r,
+                          TV* __restrict__ z) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ndim; g += gridDim.x * blockDim.x) {
+        const int q = g2r[g];
+        z[g] = q >= 0 ? TV(dr[g] * red[q]) : (isdry[g] == 2 ? TV(0) : r[g]);
+    }
+}
+
 __global__ void k_fill(int n, double v, double* __restrict__ a) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) a[q] = v;
 }
@@ -1229,6 +1423,48 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         for (int g = 0; g < 4; ++g) lu.group_start[g].push_back(int(gitems[g].size()));
     }
     for (int g = 0; g < 4; ++g) lu.d_group_items[g] = upload(lu, gitems[g], s);
+    // transposed solve: partial buffers per stage (columns x row chunks) and
+    // work items per launch group: G/H layout fuses UINV^T+H^T (group 0) and
+    // LINV^T+G^T (group 3); the L21/U12 layout runs four separate groups
+    for (int st = 0; st < 4; ++st) {
+        std::vector<int64_t> off(plan.nfronts, 0);
+        int64_t poff = 0;
+        for (int f = 0; f < plan.nfronts; ++f) {
+            const FrontDev& fr = plan.fronts[f];
+            int r0, r1, c0, c1;
+            tstage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
+            off[f] = poff;
+            poff += int64_t(c1 - c0) * ((r1 - r0 + TROWS - 1) / TROWS);
+        }
+        lu.d_tstage_off[st] = upload(lu, off, s);
+        const size_t pb = sizeof(double) * size_t(std::max<int64_t>(poff, 1));
+        lu.d_tstage_part[st] = static_cast<double*>(dmalloc(lu, pb));
+        ck(cudaMemsetAsync(lu.d_tstage_part[st], 0, pb, s));
+    }
+    {
+        const int tgroup_of[4] = {0, lu.gh ? 0 : 1, lu.gh ? 3 : 2, 3};   // TS_UINV, TS_U12, TS_LINV, TS_L21
+        std::vector<WorkItem> titems[4];
+        for (int g = 0; g < 4; ++g) lu.tgroup_start[g].assign(1, 0);
+        for (int h = 0; h < plan.nlevels; ++h) {
+            for (int st = 0; st < 4; ++st) {
+                const int g = tgroup_of[st];
+                for (int f : plan.level_fronts[h]) {
+                    const FrontDev& fr = plan.fronts[f];
+                    int r0, r1, c0, c1;
+                    tstage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
+                    for (int r = r0, ch = 0; r < r1; r += TROWS, ++ch)
+                        for (int c = c0; c < c1; c += TCOLS) {
+                            // skip tiles with no entry of a triangular part
+                            if (st == TS_UINV && r > c + TCOLS - 1) continue;        // needs r <= c
+                            if (st == TS_LINV && r + TROWS <= c) continue;           // needs r >= c (diag: r == c)
+                            titems[g].push_back(WorkItem{f, r, c, ch, st});
+                        }
+                }
+            }
+            for (int g = 0; g < 4; ++g) lu.tgroup_start[g].push_back(int(titems[g].size()));
+        }
+        for (int g = 0; g < 4; ++g) lu.d_tgroup_items[g] = upload(lu, titems[g], s);
+    }
     // factorisation scratch (per level, per front) for G/H
     std::vector<int64_t> scg;
     int64_t mx = 0;
@@ -1573,6 +1809,69 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
     ck(cudaGetLastError());
+}
+
+static TStageBufs tstage_bufs(NdLu& lu) {
+    TStageBufs sb;
+    for (int st = 0; st < 4; ++st) {
+        sb.part[st] = lu.d_tstage_part[st];
+        sb.off[st] = lu.d_tstage_off[st];
+    }
+    return sb;
+}
+template <class T>
+static void launch_tgroup(NdLu& lu, int g, int h, const T* front, double* WP, cudaStream_t s) {
+    const int ni = lu.tgroup_start[g][h + 1] - lu.tgroup_start[g][h];
+    if (!ni) return;
+    k_tgemv_part<T><<<ni, 256, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_tgroup_items[g]) +
+                                           lu.tgroup_start[g][h], front, WP, tstage_bufs(lu)); IEMIC_COUNT_LAUNCH();
+}
+template <class T, int B, class TV>
+static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    double* red = static_cast<double*>(lu.d_red);
+    double* W = static_cast<double*>(lu.d_w);
+    double* WP = static_cast<double*>(lu.d_wp);
+    const T* front = static_cast<const T*>(lu.d_front);
+    const TStageBufs sb = tstage_bufs(lu);
+    k_treduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_dc, r, red); IEMIC_COUNT_LAUNCH();
+    for (int h = 0; h < P.nlevels; ++h) {
+        const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+        const int* lf = lu.d_level_fronts + lu.level_start[h];
+        const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr);
+        k_tfwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, red, W, WP); IEMIC_COUNT_LAUNCH();
+        if (lu.gh) {
+            launch_tgroup<T>(lu, 0, h, front, WP, s);   // UINV^T and H^T on c
+            k_tfwd_reduce<2><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
+        } else {
+            launch_tgroup<T>(lu, 0, h, front, WP, s);   // v = UINV^T c
+            k_tfwd_reduce<0><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
+            launch_tgroup<T>(lu, 1, h, front, WP, s);   // -U12^T v
+            k_tfwd_reduce<1><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
+        }
+    }
+    for (int h = P.nlevels - 1; h >= 0; --h) {
+        const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+        const int* lf = lu.d_level_fronts + lu.level_start[h];
+        const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr), gN((P.level_maxnf[h] + NT - 1) / NT, nfr);
+        k_tbwd_gather<<<gF, NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
+        if (lu.gh) {
+            launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T v and -G^T y_B
+        } else {
+            launch_tgroup<T>(lu, 2, h, front, WP, s);   // -L21^T y_B
+            k_tbwd_reduce<0><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
+            launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T t
+        }
+        k_tbwd_reduce<1><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, lu.gh ? 1 : 0, B); IEMIC_COUNT_LAUNCH();
+    }
+    k_texpand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dr, red, r, z); IEMIC_COUNT_LAUNCH();
+    ck(cudaGetLastError());
+}
+
+void ndlu_apply_transpose(NdLu& lu, const double* r, double* z, cudaStream_t s) {
+    if (!lu.factored) throw EngineError(IEMIC_ERR_STATE);
+    if (lu.prec) apply_transpose_t<float, 32, double>(lu, r, z, s);
+    else apply_transpose_t<double, 32, double>(lu, r, z, s);
 }
 
 void ndlu_apply(NdLu& lu, const int* rp, const int* ci, const double* values, const void* r, void* z, int vec_fp32,

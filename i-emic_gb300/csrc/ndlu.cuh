@@ -80,6 +80,11 @@ struct NdLu {
     std::vector<int> group_start[4];        // per level offsets into d_group_items
     std::vector<double> group_bytes[4];     // per level: factor bytes the group reads
     int64_t* d_sc_gh = nullptr;             // G/H scratch offsets per front (by level)
+    // transposed solve: partial buffers per transposed stage, items per group
+    double* d_tstage_part[4] = {nullptr, nullptr, nullptr, nullptr};
+    int64_t* d_tstage_off[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* d_tgroup_items[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<int> tgroup_start[4];
     // recursive triangular inversion: tasks, tiles, per level the tile ranges
     // of its launches, and the scratch of the first product of each merge
     void *d_tri_tasks = nullptr, *d_tri_tiles = nullptr, *d_tri_scratch = nullptr;
@@ -102,5 +107,8 @@ void ndlu_factor(NdLu& lu, const int* row_ptr, const int* col_idx, const double*
 // triangular solves accumulate in FP64 whatever the factor precision.
 void ndlu_apply(NdLu& lu, const int* row_ptr, const int* col_idx, const double* values, const void* r, void* z,
                 int vec_fp32, cudaStream_t s);
+// z = M^{-T} r with the same factors (FP64 vectors): the transposed
+// preconditioner of J^T for adjoint solves.
+void ndlu_apply_transpose(NdLu& lu, const double* r, double* z, cudaStream_t s);
 
 }  // namespace iemic

@@ -358,6 +358,7 @@ void Engine::jacobian_dev(const double* x) {
     ck(cudaGetLastError());
     jac_valid = true;
     fact64_stale = fact32_stale = true;
+    jacT_stale = true;
 }
 
 // ---------------------------------------------------------------------------

@@ -72,6 +72,7 @@ struct Pattern {
 // launchers (thcm_assembly.cu)
 void launch_lin(const Geo& g, const Params& p, double* al_tab, cudaStream_t s);
 void launch_usol(const Geo& g, const double* x, double* pads, cudaStream_t s);
+void launch_dfdsurf_t(const Geo& g, const ForcingScalars& fs, const double* lambda, double* grad, cudaStream_t s);
 void launch_pattern(const Geo& g, const Pattern& pat, int* col_idx, cudaStream_t s);
 void launch_jacobian(const Geo& g, const Params& p, const Pattern& pat, const double* al_tab,
                      const double* pads, double* val, float* val32, cudaStream_t s);

@@ -732,4 +732,47 @@ void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s) {
     mass_kernel<<<grid_for(nc, 256), 256, 0, s>>>(g, p.par[ROSB], diagB); IEMIC_COUNT_LAUNCH();
 }
 
+
+// ---------------------------------------------------------------------------
+// Adjoint of the surface forcing: grad[f][i,j] = -lambda^T dF/d(field f)(i,j)
+// for f = taux, tauy, tatm, emip, spert. F is affine in these fields and
+// every field value enters one row only, the row forcing_row fills (with the
+// same land and boundary conditions): F_row = -(frc_row - acc) (1 - landm).
+// ---------------------------------------------------------------------------
+__global__ void dfdsurf_t_kernel(Geo g, ForcingScalars fs, const double* __restrict__ lambda,
+                                 double* __restrict__ grad) {
+    const int nm = g.n * g.m;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 5 * nm; q += gridDim.x * blockDim.x) {
+        const int f = q / nm, ij = q % nm;
+        const int i = ij % g.n + 1, j = ij / g.n + 1, k = g.l;
+        const Nb nb = load_nb(g, i, j, k);
+        double coef = 0.0;
+        int A = 0;
+        if (nb.c[5] == OCEAN) {
+            if (f <= 1) {
+                if (!(nb.c[6] == LAND || nb.c[8] == LAND || nb.c[9] == LAND) && j <= g.m - 1) {
+                    coef = fs.sigma;
+                    A = f == 0 ? UU : VV;
+                }
+            } else if (f == 2) {
+                coef = fs.etabi;
+                A = TT;
+            } else {
+                coef = f == 3 ? fs.gamma * (1 - fs.hmtp) : fs.sper_fac;
+                A = SS;
+            }
+        }
+        double v = 0.0;
+        if (A) {
+            const size_t row = size_t(NUN) * (size_t(i - 1) + size_t(g.n) * (size_t(j - 1) + size_t(g.m) * (k - 1))) + A - 1;
+            // dF_row / dfield = -coef (1 - landm); dg/dfield = -lambda_row dF_row/dfield
+            v = lambda[row] * coef * double(1 - g.L(i, j, k));
+        }
+        grad[q] = v;
+    }
+}
+void launch_dfdsurf_t(const Geo& g, const ForcingScalars& fs, const double* lambda, double* grad, cudaStream_t s) {
+    dfdsurf_t_kernel<<<grid_for(size_t(5) * g.n * g.m, 256), 256, 0, s>>>(g, fs, lambda, grad); IEMIC_COUNT_LAUNCH();
+}
+
 }  // namespace iemic

@@ -23,7 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompi
           "-Xcompiler", "-fno-strict-aliasing", "-Xcompiler", "-ffp-contract=off"]
 # per-file extra flags
 EXTRA = {"thcm_assembly.cu": ["-fmad=false"]}
-SOURCES = ["ocean.cu", "thcm_assembly.cu", "krylov.cu", "ndlu.cu", "solver.cu", "continuation.cu", "noalloc.cu"]
+SOURCES = ["ocean.cu", "thcm_assembly.cu", "krylov.cu", "ndlu.cu", "solver.cu", "continuation.cu", "noalloc.cu", "adjoint.cu"]
 
 
 def nvcc():

@@ -104,6 +104,18 @@ class KernelStats(ctypes.Structure):
                 ("flops", ctypes.c_double)]
 
 
+class AdjointOpts(ctypes.Structure):
+    _fields_ = [("i_begin", ctypes.c_int), ("i_end", ctypes.c_int), ("solve", SolveOpts), ("fd_rel", ctypes.c_double)]
+
+
+class AdjointStats(ctypes.Structure):
+    _fields_ = [("g", ctypes.c_double), ("jmax", ctypes.c_int), ("kmax", ctypes.c_int), ("iters", ctypes.c_int),
+                ("relres", ctypes.c_double), ("time_ms", ctypes.c_double)]
+
+
+FORCING_FIELDS = ("taux", "tauy", "tatm", "emip", "spert")
+
+
 class SolverInfo(ctypes.Structure):
     _fields_ = [("unknowns", ctypes.c_int64), ("reduced_unknowns", ctypes.c_int64), ("fronts", ctypes.c_int64),
                 ("levels", ctypes.c_int64), ("factor_entries", ctypes.c_int64), ("front_entries", ctypes.c_int64),
@@ -146,6 +158,13 @@ SIGNATURES = {
     "iemic_solve_dev": [_VP, _VP, _VP, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats)],
     "iemic_solver_gauge": [_VP, _IP, ctypes.c_int, _IP],
     "iemic_get_solver_info": [_VP, ctypes.POINTER(SolverInfo)],
+    "iemic_psim": [_VP, _DP, _DP, _DP, _DP],
+    "iemic_psim_max_grad_dev": [_VP, _VP, ctypes.c_int, ctypes.c_int, _DP, _IP, _VP],
+    "iemic_forcing_adjoint_dev": [_VP, _VP, _VP],
+    "iemic_par_adjoint_dev": [_VP, _VP, _VP, ctypes.c_int, ctypes.c_double, _DP],
+    "iemic_default_adjoint_opts": [ctypes.POINTER(AdjointOpts)],
+    "iemic_adjoint_psim": [_VP, _DP, ctypes.POINTER(AdjointOpts), _DP, _IP, ctypes.c_int, _DP,
+                           ctypes.POINTER(AdjointStats)],
     "iemic_kernel_timing": [_VP, ctypes.c_int],
     "iemic_kernel_stats_get": [_VP, ctypes.c_int, ctypes.POINTER(KernelStats)],
     "iemic_get_stream": [_VP, ctypes.POINTER(_VP)],
@@ -158,7 +177,8 @@ SIGNATURES = {
                                    ctypes.POINTER(ContinuationStats)],
     "iemic_launch_count": [],
 }
-_VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts"}
+_VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts",
+                "iemic_default_adjoint_opts"}
 
 _lib = None
 
@@ -439,3 +459,41 @@ class Ocean:
         p = _VP()
         self._check(self.L.iemic_get_stream(self._h, ctypes.byref(p)), "stream")
         return p.value or 0
+
+    # ---- diagnostics and adjoint ---------------------------------------------
+    def getPsiM(self, x=None):
+        """Ocean::getPsiM: (psi (l+1, m+1) in Sv, psiMin, psiMax)."""
+        x = np.ascontiguousarray(self.state if x is None else x, dtype=np.float64)
+        psi = np.zeros((self.l + 1) * (self.m + 1))
+        lo, hi = ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.iemic_psim(self._h, _dp(x), _dp(psi), ctypes.byref(lo), ctypes.byref(hi)), "getPsiM")
+        return psi.reshape(self.l + 1, self.m + 1), lo.value, hi.value
+
+    def default_adjoint_opts(self, precision=PREC_MIXED):
+        o = AdjointOpts()
+        self.L.iemic_default_adjoint_opts(ctypes.byref(o))
+        o.solve.precision = precision
+        return o
+
+    def adjointPsiM(self, x, pars=(), sector=None, opts=None, **kw):
+        """Gradient of g = max psi_M (Sv) at the steady state x: returns
+        (g, {field: (m, n) gradient}, {par: gradient}, stats)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        o = opts if opts is not None else self.default_adjoint_opts(kw.pop("precision", PREC_MIXED))
+        if sector is not None:
+            o.i_begin, o.i_end = sector
+        for k, v in kw.items():
+            setattr(o.solve, k, v)
+        idx = np.array([self.par2int(p) for p in pars], dtype=np.int32)
+        gp = np.zeros(max(len(idx), 1))
+        gf = np.zeros(5 * self.n * self.m)
+        st = AdjointStats()
+        rc = self.L.iemic_adjoint_psim(self._h, _dp(x), ctypes.byref(o), _dp(gf), _ip(idx) if len(idx) else None,
+                                       len(idx), _dp(gp), ctypes.byref(st))
+        stats = _asdict(st)
+        stats["status"] = rc
+        if rc not in (0, -3):
+            raise IemicError(rc, "adjointPsiM")
+        fields = {name: gf[q * self.n * self.m:(q + 1) * self.n * self.m].reshape(self.m, self.n)
+                  for q, name in enumerate(FORCING_FIELDS)}
+        return st.g, fields, {p: gp[q] for q, p in enumerate(pars)}, stats

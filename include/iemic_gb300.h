@@ -222,6 +222,44 @@ int iemic_continuation_run(iemic_ocean* h, double* x, const iemic_continuation_o
 int iemic_continuation_run_dev(iemic_ocean* h, double* x_dev, const iemic_continuation_opts* o,
                                iemic_continuation_stats* st);
 
+/* ---- adjoint -----------------------------------------------------------
+ * Ocean::getPsiM (src/ocean/Ocean.C:882-896; OceanGrid::recomputePsiM,
+ * src/ocean/OceanGrid.C:268-340; compute_psim, src/ocean/thcm_utils.F90:95-118):
+ * the meridional overturning streamfunction psi(j,k), (m+1)(l+1) values
+ * psim[(m+1)k + j], and its extrema, in Sv. */
+int iemic_psim(iemic_ocean* h, const double* x, double* psim, double* psi_min, double* psi_max);
+/* No reference counterpart (the adjoint is new): g = max psi over the
+ * longitude sector [i_begin, i_end) and dg/dx (device vector); jk[0..1] =
+ * (j, k) of the maximum. */
+int iemic_psim_max_grad_dev(iemic_ocean* h, const double* x_dev, int i_begin, int i_end, double* g, int* jk,
+                            double* grad_dev);
+/* -lambda^T dF/d(surface field) for the 5 fields taux, tauy, tatm, emip,
+ * spert of iemic_set_forcing (5*n*m values, field-major, i fastest): the
+ * gradient of g with respect to the forcing when J^T lambda = dg/dx. */
+int iemic_forcing_adjoint_dev(iemic_ocean* h, const double* lambda_dev, double* grad_dev);
+/* -lambda^T dF/dpar(par_idx) by central differences (step fd_rel max(1,|par|)). */
+int iemic_par_adjoint_dev(iemic_ocean* h, const double* x_dev, const double* lambda_dev, int par_idx, double fd_rel,
+                          double* out);
+typedef struct {
+    int i_begin, i_end;        /* longitude sector of the overturning sum; i_end < 0: to n */
+    iemic_solve_opts solve;    /* the transposed solve (transpose is set by the call) */
+    double fd_rel;             /* relative step of the parameter central differences */
+} iemic_adjoint_opts;
+typedef struct {
+    double g;                  /* max psi (Sv) */
+    int jmax, kmax;            /* where it is attained */
+    int iters;                 /* Krylov iterations of the J^T solve */
+    double relres;             /* its FP64 relative residual */
+    double time_ms;
+} iemic_adjoint_stats;
+void iemic_default_adjoint_opts(iemic_adjoint_opts* o);
+/* Gradient of g = max psi (Sv) at a steady state x (host, F(x) = 0) with
+ * respect to the surface forcing fields (grad_fields: 5*n*m host values or
+ * NULL) and the parameters par_idx[0..npar) (grad_par), by one transposed
+ * solve J^T lambda = dg/dx preconditioned with the factorisation of J. */
+int iemic_adjoint_psim(iemic_ocean* h, const double* x, const iemic_adjoint_opts* o, double* grad_fields,
+                       const int* par_idx, int npar, double* grad_par, iemic_adjoint_stats* st);
+
 /* Device timing of the instrumented kernel classes (no reference
  * counterpart; it plays the role of the reference's TIMER_START/STOP
  * profile, src/globaldefs/GlobalDefinitions.H:193-223). enable = 1 clears the
