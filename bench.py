@@ -13,8 +13,8 @@ Every linear solve reaches ||b - J x|| <= 1e-8 ||b|| and every corrector
 
 A "step" is one continuation step (predictor plus Newton corrector); the
 metric counts Newton corrector iterations (one Jacobian, three residuals,
-one preconditioner rebuild, two solves and the update each) per second of
-device time. ``--impl reference`` times the CPU restatement of the same
+one preconditioner rebuild, the bordered solve(s) and the update each) per
+second of device time. ``--impl reference`` times the CPU restatement of the same
 Newton iteration (C++ oracle assembly + numpy/LAPACK multifrontal LU) on the
 host cores; it is the CPU baseline, not the target.
 """
@@ -63,12 +63,15 @@ def workload(name):
 
 
 def continuation_opts(ocean, precision, steps, fscale):
-    """Freshwater-forcing continuation: the step sizes and Newton limits of the
-    reference's parameterfiles/continuation_params.xml, residual test 'R'."""
+    """Freshwater-forcing continuation with the reference's test settings
+    (test/ocean/continuation_params.xml: step sizes 1e-2 / 1e-8 / 1e-1, 15
+    Newton iterations, epsilon 1e-5, secant tangent, Newton-chord hybrid,
+    predictor bound 3000) and the corrector converged to
+    ||F||_2 <= 1e-8 ||F(0)||_2 (residual test 'R')."""
     return ocean.default_continuation_opts("Salinity Forcing", precision), dict(
         ds=0.01, ds_min=1e-8, ds_max=0.1, destination=10.0, max_steps=steps, max_newton=15, min_newton=1,
-        opt_newton=4.0, newton_tol=1e-8 * fscale, residual_test=b"R", normalize=b"N", tangent=b"S",
-        predictor_bound=1e30, tan_scaling=1.0)
+        opt_newton=3.5, newton_tol=1e-8 * fscale, residual_test=b"R", normalize=b"N", tangent=b"S",
+        newton_chord=1, epsilon=1e-5, predictor_bound=3000.0, tan_scaling=1.0)
 
 
 def dist_init():
@@ -175,6 +178,8 @@ def roofline(stats, peaks):
         except (OSError, ValueError):
             pass
     out["classes"] = {k: {"ms": v["ms"], "launches": v["launches"]} for k, v in stats.items()}
+    out["timing"] = ("CUDA events around every launch on the launching stream, in an instrumented repeat of "
+                     "the timed mixed steps from the same starting point")
     return out
 
 
@@ -304,7 +309,6 @@ def run_ours(args, rank, world):
             dist.barrier()
         timing = label == "mixed"
         if timing:
-            oc.kernelTiming(True)
             clocks = Clocks()
             n0 = L.iemic_launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -317,13 +321,22 @@ def run_ours(args, rank, world):
         if timing:
             launches = L.iemic_launch_count() - n0
             clk = clocks.stop()
-            kstats = oc.kernelStats()
-            oc.kernelTiming(False)
         ms = barrier_max(ms, world)
         iters = barrier_sum(st["newton_iters"], world)
         results[label] = dict(ms=ms, newton_iters=iters, stats=st, value=iters / (ms * 1e-3))
         if timing:
-            results[label].update(launches=launches, clocks=clk, kstats=kstats)
+            results[label].update(launches=launches, clocks=clk)
+
+    # --- per-kernel device times: the timed mixed steps repeated from the same
+    # point with CUDA events around every launch (eager launches, on the stream
+    # the kernels run on), so the timed region above stays uninstrumented
+    x = x_start.clone()
+    oc.setPar("Salinity Forcing", par_w)
+    oc.kernelTiming(True)
+    cont_dev(x, 1, args.steps)
+    torch.cuda.synchronize()
+    results["mixed"]["kstats"] = oc.kernelStats()
+    oc.kernelTiming(False)
 
     # --- end to end through the public API with host buffers (mixed path)
     e2e = None

@@ -92,6 +92,9 @@ struct NdLu {
     double tri_flops = 0.0;
     void* d_scratch = nullptr;
     cudaGraphExec_t sweep_exec = nullptr; // captured forward + backward level sweeps
+    cudaGraphExec_t factor_exec = nullptr;  // captured factorisation
+    long long factor_launches = 0;
+    const void *fg_rp = nullptr, *fg_ci = nullptr, *fg_val = nullptr;   // arrays the factor graph reads
     long long sweep_launches = 0;           // kernels in the captured sweeps
     int npert = 0;
     bool factored = false;
