@@ -429,103 +429,91 @@ __global__ void k_extend_add(const FrontDev* __restrict__ fronts, const int* __r
 // unit-lower and upper factors. With the barotropic pressures deferred to the
 // root, no fully-summed block is singular and local pivots suffice.
 template <class T, int B>
-__global__ void k_panel_diag(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int p,
-                             T* __restrict__ front, T* __restrict__ dinv, int* __restrict__ piv, T tau,
-                             int* __restrict__ npert) {
+__global__ void __launch_bounds__(32) k_panel_diag(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                                   int p, T* __restrict__ front, T* __restrict__ dinv,
+                                                   int* __restrict__ piv, T tau, int* __restrict__ npert) {
+    // One warp per front; lane r holds row r of the bb x bb diagonal block in
+    // registers (all loops fully unrolled, so the row stays in registers).
+    // Pivot search, row maxima and the broadcast of the pivot row are warp
+    // shuffles; there is no shared-memory round trip in the elimination.
+    static_assert(B == 32, "one lane per row");
     const FrontDev fr = fronts[lf[blockIdx.x]];
     if (fr.nf <= p) return;
-    const int bb = min(B, fr.nf - p), F = fr.F, tid = threadIdx.x;
-    T* A = front + fr.off;
-    __shared__ T S[B][B + 1];
-    __shared__ T X[B][B + 1];
-    __shared__ int perm[B];
-    __shared__ int prow;
-    for (int e = tid; e < bb * bb; e += blockDim.x) {
-        int r = e % bb, c = e / bb;
-        S[r][c] = A[int64_t(p + c) * F + p + r];
-    }
-    if (tid < bb) perm[tid] = tid;
-    __syncthreads();
-    for (int j = 0; j < bb; ++j) {
-        if (tid < 32) {
-            T bv = T(-1);
-            int br = j;
-            for (int r = j + tid; r < bb; r += 32) {
-                T v = abs(S[r][j]);
-                if (v > bv) { bv = v; br = r; }
-            }
+    const int bb = min(B, fr.nf - p), F = fr.F, lane = threadIdx.x;
+    const unsigned full = 0xffffffffu;
+    T* A = front + fr.off + int64_t(p) * F + p;
+    T row[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) row[c] = (lane < bb && c < bb) ? A[int64_t(c) * F + lane] : (lane == c ? T(1) : T(0));
+    int perm = lane;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+        if (j < bb) {
+            // pivot: largest |row[j]| over lanes j..bb-1, smallest lane on ties
+            T bv = (lane >= j && lane < bb) ? abs(row[j]) : T(-1);
+            int br = lane;
+#pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                T ov = __shfl_xor_sync(0xffffffffu, bv, o);
-                int orr = __shfl_xor_sync(0xffffffffu, br, o);
+                const T ov = __shfl_xor_sync(full, bv, o);
+                const int orr = __shfl_xor_sync(full, br, o);
                 if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
             }
-            if (tid == 0) prow = br;
-        }
-        __syncthreads();
-        const int pr = prow;
-        if (pr != j) {
-            for (int c = tid; c < bb; c += blockDim.x) {
-                T t = S[j][c];
-                S[j][c] = S[pr][c];
-                S[pr][c] = t;
+            const int pr = br;
+            if (pr != j) {   // swap rows j and pr (uniform branch)
+                const int src = lane == j ? pr : (lane == pr ? j : lane);
+#pragma unroll
+                for (int c = 0; c < B; ++c) row[c] = __shfl_sync(full, row[c], src);
+                perm = __shfl_sync(full, perm, src);
             }
-            if (tid == 0) {
-                int t = perm[j];
-                perm[j] = perm[pr];
-                perm[pr] = t;
+            // pivot row maximum from column j on
+            T sc = T(0);
+#pragma unroll
+            for (int c = j; c < B; ++c) sc = max(sc, abs(row[c]));
+            sc = __shfl_sync(full, (lane < bb) ? sc : T(0), j);
+            T d = __shfl_sync(full, row[j], j);
+            if (!(abs(d) > tau * sc)) {
+                d = (d < T(0) ? -tau : tau) * (sc > T(0) ? sc : T(1));
+                if (lane == j) {
+                    row[j] = d;
+                    atomicAdd(npert, 1);
+                }
             }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            T scale = T(0);
-            for (int c = j; c < bb; ++c) scale = max(scale, abs(S[j][c]));
-            if (!(abs(S[j][j]) > tau * scale)) {
-                S[j][j] = (S[j][j] < T(0) ? -tau : tau) * (scale > T(0) ? scale : T(1));
-                atomicAdd(npert, 1);
+            if (lane > j && lane < bb) row[j] /= d;
+#pragma unroll
+            for (int c = j + 1; c < B; ++c) {
+                const T u = __shfl_sync(full, row[c], j);
+                if (lane > j && lane < bb && c < bb) row[c] -= row[j] * u;
             }
-        }
-        __syncthreads();
-        const T d = S[j][j];
-        for (int r = j + 1 + tid; r < bb; r += blockDim.x) S[r][j] /= d;
-        __syncthreads();
-        const int w = bb - j - 1;
-        for (int e = tid; e < w * w; e += blockDim.x) {
-            int r = j + 1 + e % w, c = j + 1 + e / w;
-            S[r][c] -= S[r][j] * S[j][c];
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < bb * bb; e += blockDim.x) {
-        int r = e % bb, c = e / bb;
-        A[int64_t(p + c) * F + p + r] = S[r][c];
-    }
-    if (tid < bb) piv[fr.red0 + p + tid] = perm[tid];
-    if (tid < bb) {   // inverse of the unit-lower factor
-        const int c = tid;
-        for (int r = 0; r < bb; ++r) X[r][c] = T(0);
-        X[c][c] = T(1);
-        for (int r = c + 1; r < bb; ++r) {
-            T s = T(0);
-            for (int q = c; q < r; ++q) s += S[r][q] * X[q][c];
-            X[r][c] = -s;
         }
     }
-    __syncthreads();
+    if (lane < bb) {
+#pragma unroll
+        for (int c = 0; c < B; ++c)
+            if (c < bb) A[int64_t(c) * F + lane] = row[c];
+        piv[fr.red0 + p + lane] = perm;
+    }
+    // inverses: lane c computes column c of Linv (unit lower) and of Uinv
     T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
-    for (int e = tid; e < B * B; e += blockDim.x) Di[e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
-    __syncthreads();
-    if (tid < bb) {   // inverse of the upper factor
-        const int c = tid;
-        for (int r = 0; r < bb; ++r) X[r][c] = T(0);
-        X[c][c] = T(1) / S[c][c];
-        for (int r = c - 1; r >= 0; --r) {
-            T s = T(0);
-            for (int q = r + 1; q <= c; ++q) s += S[r][q] * X[q][c];
-            X[r][c] = -s / S[r][r];
-        }
+    T x[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+        T t = (r == lane) ? T(1) : T(0);
+#pragma unroll
+        for (int q = 0; q < r; ++q) t -= __shfl_sync(full, row[q], r) * x[q];   // L[r][q] from lane r
+        x[r] = (r > lane) ? t : (r == lane ? T(1) : T(0));
     }
-    __syncthreads();
-    for (int e = tid; e < B * B; e += blockDim.x) Di[B * B + e] = (e / B < bb && e % B < bb) ? X[e / B][e % B] : T(0);
+#pragma unroll
+    for (int r = 0; r < B; ++r) Di[r * B + lane] = (r < bb && lane < bb) ? x[r] : T(0);
+#pragma unroll
+    for (int r = B - 1; r >= 0; --r) {
+        const T urr = __shfl_sync(full, row[r], r);
+        T t = (r == lane) ? T(1) : T(0);
+#pragma unroll
+        for (int q = r + 1; q < B; ++q) t -= __shfl_sync(full, row[q], r) * x[q];   // U[r][q] from lane r
+        x[r] = (r <= lane && r < bb && lane < bb) ? t / urr : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < B; ++r) Di[B * B + r * B + lane] = (r < bb && lane < bb) ? x[r] : T(0);
 }
 
 // The block row permutation of panel p applied to every column outside the
@@ -862,12 +850,31 @@ __global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* _
 // and the K loop skips their zero part.
 enum { OP_DENSE = 0, OP_LOWER_UNIT = 1, OP_UPPER = 2 };
 constexpr int TRI_SB = 256;   // super-block rows of the row-oriented steps
+constexpr int TRI_KS = 512;   // K piece of a split-K product
 struct TriTask {
     int64_t a_off, b_off, c_off;   // element offsets: base 0 = front storage, 1 = scratch
     int lda, ldb, ldc, M, N, K;
     int opA, opB, a_base, b_base, c_base;
     float alpha;
+    int k0 = 0, k1 = 1 << 30;      // K sub-range of a split-K part
 };
+// Split-K partial sums of one product: part s (s = 1..nsplit-1) lies at
+// off + s * len and is added into part 0 at off.
+struct SplitGroup {
+    int64_t off, len;
+    int nsplit;
+};
+template <class T>
+__global__ void k_split_reduce(const SplitGroup* __restrict__ groups, int ngroups, T* __restrict__ scr) {
+    for (int g = blockIdx.y; g < ngroups; g += gridDim.y) {
+        const SplitGroup sg = groups[g];
+        for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < sg.len; q += int64_t(gridDim.x) * blockDim.x) {
+            T v = scr[sg.off + q];
+            for (int sp = 1; sp < sg.nsplit; ++sp) v += scr[sg.off + sp * sg.len + q];
+            scr[sg.off + q] = v;
+        }
+    }
+}
 struct TriTile {
     int task, i0, j0;
 };
@@ -886,7 +893,7 @@ __global__ void __launch_bounds__(256) k_tri_gemm(const TriTask* __restrict__ ta
     const T* Bm = (t.b_base ? scr : front) + t.b_off;
     T* C = (t.c_base ? scr : front) + t.c_off;
     const int i0 = tl.i0, j0 = tl.j0;
-    int kb = 0, ke = t.K;
+    int kb = max(0, t.k0), ke = min(t.K, t.k1);
     if (t.opA == OP_LOWER_UNIT) ke = min(ke, i0 + 64);
     if (t.opA == OP_UPPER) kb = max(kb, i0);
     if (t.opB == OP_LOWER_UNIT) kb = max(kb, j0);
@@ -936,72 +943,111 @@ __global__ void __launch_bounds__(256) k_tri_gemm(const TriTask* __restrict__ ta
     }
 }
 
-// G = L21 * Linv11 (rows nf:F) or H = Uinv11 * U12 (columns nf:F), 64x64 tiles into scratch
-template <class T, bool HMAT>
-__global__ void __launch_bounds__(256) k_gh(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                            const T* __restrict__ front, T* __restrict__ scratch,
-                                            const int64_t* __restrict__ sc_off) {
-    const FrontDev fr = fronts[lf[blockIdx.y]];
-    const int nf = fr.nf, nb = fr.nb, F = fr.F;
-    if (nf == 0 || nb == 0) return;
-    const int M = HMAT ? nf : nb, N = HMAT ? nb : nf;
-    const int tm = (M + 63) / 64, tn = (N + 63) / 64;
-    if (int(blockIdx.x) >= tm * tn) return;
-    const int i0 = (blockIdx.x % tm) * 64, j0 = (blockIdx.x / tm) * 64;
-    const T* A = front + fr.off;
-    __shared__ T As[32][65];
-    __shared__ T Bs[32][65];
+// FP32 task GEMM (triangular inversion and G/H): C = alpha op(A) op(B) over
+// 128 x 128 tiles with the staging of k_fgemm_f32 (cp.async double buffering,
+// float4 operands, swizzled B). Masked triangular entries are zero-filled by
+// the copy; the implicit unit diagonal of OP_LOWER_UNIT operands is written
+// into shared memory by the thread that issued its copy, after its copies
+// completed and before the barrier that publishes the chunk.
+__device__ __forceinline__ bool tri_mask(int op, int r, int c) {
+    return op == OP_DENSE || (op == OP_LOWER_UNIT ? r > c : r <= c);
+}
+__global__ void __launch_bounds__(256, 2) k_task_gemm_f32(const TriTask* __restrict__ tasks,
+                                                          const TriTile* __restrict__ tiles,
+                                                          float* __restrict__ front, float* __restrict__ scr) {
+    constexpr int TM = FG_TM;
+    const TriTile tl = tiles[blockIdx.x];
+    const TriTask t = tasks[tl.task];
+    const float* A = (t.a_base ? scr : front) + t.a_off;
+    const float* Bm = (t.b_base ? scr : front) + t.b_off;
+    float* C = (t.c_base ? scr : front) + t.c_off;
+    const int i0 = tl.i0, j0 = tl.j0;
+    int kb = max(0, t.k0), ke = min(t.K, t.k1);
+    if (t.opA == OP_LOWER_UNIT) ke = min(ke, i0 + TM);
+    if (t.opA == OP_UPPER) kb = max(kb, i0);
+    if (t.opB == OP_LOWER_UNIT) kb = max(kb, j0);
+    if (t.opB == OP_UPPER) ke = min(ke, j0 + TM);
+    extern __shared__ __align__(16) float fg_smem[];
+    auto As = [&](int buf, int k) { return fg_smem + (buf * 32 + k) * TM; };
+    auto Bs = [&](int buf, int k) { return fg_smem + 2 * 32 * TM + (buf * 32 + k) * TM; };
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    T acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
-    // G(r, c) = sum_k L21(r, k) X(k, c), k in [c, nf): k from j0
-    // H(r, c) = sum_k Y(r, k) U12(k, c), k in [r, nf): k from i0
-    const int kb = HMAT ? i0 : j0;
-    for (int k0 = kb; k0 < nf; k0 += 32) {
-        for (int e = tid; e < 32 * 64; e += 256) {
-            int ii = e % 64, kk = e / 64;
-            int r = i0 + ii, k = k0 + kk;
-            T v = T(0);
-            if (r < M && k < nf) v = HMAT ? opld<T, MD_UPPER>(A, F, r, k) : A[int64_t(k) * F + nf + r];
-            As[kk][ii] = v;
+    auto issue = [&](int k0c, int buf) {
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+            const int e = tid + 256 * q, i = e % TM, k = e / TM, r = i0 + i, kk = k0c + k;
+            const bool v = r < t.M && kk < ke && tri_mask(t.opA, r, kk);
+            cp_async4(As(buf, k) + i, v ? A + int64_t(kk) * t.lda + r : A, v);
         }
-        for (int e = tid; e < 32 * 64; e += 256) {
-            int kk = e % 32, jj = e / 32;
-            int k = k0 + kk, c = j0 + jj;
-            T v = T(0);
-            if (c < N && k < nf) v = HMAT ? A[int64_t(nf + c) * F + k] : opld<T, MD_LOWER_UNIT>(A, F, k, c);
-            Bs[kk][jj] = v;
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+            const int e = tid + 256 * q, k = e % 32, j = e / 32, c = j0 + j, kk = k0c + k;
+            const bool v = c < t.N && kk < ke && tri_mask(t.opB, kk, c);
+            cp_async4(Bs(buf, k) + ((((j >> 2) ^ (k & 7)) << 2) | (j & 3)), v ? Bm + int64_t(c) * t.ldb + kk : Bm, v);
         }
+        cp_async_commit();
+    };
+    auto unit_diag = [&](int k0c, int buf) {   // after this thread's copies of the chunk completed
+        if (t.opA == OP_LOWER_UNIT) {
+#pragma unroll 4
+            for (int q = 0; q < 16; ++q) {
+                const int e = tid + 256 * q, i = e % TM, k = e / TM, r = i0 + i, kk = k0c + k;
+                if (r == kk && r < t.M && kk < ke) As(buf, k)[i] = 1.f;
+            }
+        }
+        if (t.opB == OP_LOWER_UNIT) {
+#pragma unroll 4
+            for (int q = 0; q < 16; ++q) {
+                const int e = tid + 256 * q, k = e % 32, j = e / 32, c = j0 + j, kk = k0c + k;
+                if (kk == c && c < t.N && kk < ke) Bs(buf, k)[(((j >> 2) ^ (k & 7)) << 2) | (j & 3)] = 1.f;
+            }
+        }
+    };
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    if (kb < ke) issue(kb, 0);
+    int buf = 0;
+    for (int k0c = kb; k0c < ke; k0c += 32) {
+        cp_async_wait_all();
+        unit_diag(k0c, buf);
         __syncthreads();
+        if (k0c + 32 < ke) issue(k0c + 32, buf ^ 1);
 #pragma unroll 8
-        for (int kk = 0; kk < 32; ++kk) {
-            T av[4], bv[4];
+        for (int k = 0; k < 32; ++k) {
+            const float* ar = As(buf, k);
+            const float* br = Bs(buf, k);
+            const float4 a0 = *reinterpret_cast<const float4*>(ar + tx * 4);
+            const float4 a1 = *reinterpret_cast<const float4*>(ar + 64 + tx * 4);
+            const int sw = k & 7;
+            const float4 b0 = *reinterpret_cast<const float4*>(br + ((ty ^ sw) << 2));
+            const float4 b1 = *reinterpret_cast<const float4*>(br + (((16 + ty) ^ sw) << 2));
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-            for (int a = 0; a < 4; ++a) av[a] = As[kk][tx * 4 + a];
+            for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][ty * 4 + b];
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+                for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
         }
         __syncthreads();
+        buf ^= 1;
     }
-    T* S = scratch + sc_off[blockIdx.y];
+    const float alpha = t.alpha;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        int c = j0 + ty * 4 + b;
-        if (c >= N) continue;
+    for (int b = 0; b < 8; ++b) {
+        const int c = j0 + (b < 4 ? ty * 4 + b : 64 + ty * 4 + b - 4);
+        if (c >= t.N) continue;
+        float* col = C + int64_t(c) * t.ldc;
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            int r = i0 + tx * 4 + a;
-            if (r < M) S[int64_t(c) * M + r] = acc[a][b];
+        for (int a = 0; a < 8; ++a) {
+            const int r = i0 + (a < 4 ? tx * 4 + a : 64 + tx * 4 + a - 4);
+            if (r < t.M) col[r] = alpha * acc[a][b];
         }
     }
 }
+
+// G/H are formed by k_task_gemm_f32 into scratch; the copy puts them in place of L21 / U12
 template <class T, bool HMAT>
 __global__ void k_gh_copy(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ front,
                           const T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
@@ -1169,8 +1215,20 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
     double out;
     if (sizeof(T) == 4) {
         float sh = 0.f, sl = 0.f;
-#pragma unroll 4
-        for (int c = c0; c < c1; ++c) {
+        // loads are issued 16 columns ahead of the accumulation chain so that
+        // each thread keeps 16 independent HBM reads in flight
+        int c = c0;
+        for (; c + 16 <= c1; c += 16) {
+            float a[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) a[u] = float(A[int64_t(c + u) * F]);
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const float2 xv = xs2[c + u - it.col0];
+                dd_acc(sh, sl, sg * a[u], xv.x, xv.y);
+            }
+        }
+        for (; c < c1; ++c) {
             const float2 xv = xs2[c - it.col0];
             dd_acc(sh, sl, sg * float(A[int64_t(c) * F]), xv.x, xv.y);
         }
@@ -1494,6 +1552,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_STRIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_BAND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
+    ck(cudaFuncSetAttribute(k_task_gemm_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     lu.prec = prec;
     lu.plan = &plan;
     const size_t ts = prec ? sizeof(float) : sizeof(double);
@@ -1651,15 +1710,18 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     {
         std::vector<TriTask> tasks;
         std::vector<TriTile> tiles;
+        std::vector<SplitGroup> groups;
+        const int tile = prec ? FG_TM : 64;   // k_task_gemm_f32 / k_tri_gemm tile size
         int64_t tmax = 0;
         lu.tri_ranges.clear();
+        lu.gh_ranges.clear();
         for (int h = 0; h < plan.nlevels; ++h) {
             std::vector<std::pair<int, int>> lv;
             auto emit = [&](const TriTask& t) {
                 const int id = int(tasks.size());
                 tasks.push_back(t);
-                for (int j = 0; j < t.N; j += 64)
-                    for (int i = 0; i < t.M; i += 64) tiles.push_back(TriTile{id, i, j});
+                for (int j = 0; j < t.N; j += tile)
+                    for (int i = 0; i < t.M; i += tile) tiles.push_back(TriTile{id, i, j});
             };
             // (1) merges inside the 256-row super-blocks: sz = 32, 64, 128
             for (int sz = plan.panel; sz < TRI_SB && sz < plan.level_maxnf[h]; sz *= 2) {
@@ -1699,9 +1761,12 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
             //     lower, top down:  X[Ri, 0:i0] = -Linv_ii (L[Ri, 0:i0] X[0:i0, 0:i0])
             //     upper, bottom up: Y[Ri, i1:nf] = -Uinv_ii (U[Ri, i1:nf] Y[i1:nf, i1:nf])
             const int nsb_max = (plan.level_maxnf[h] + TRI_SB - 1) / TRI_SB;
+            // long products (w > TRI_KS) are split along K into TRI_KS pieces
+            auto nsplit = [](int w) { return w > 2 * TRI_KS ? (w + TRI_KS - 1) / TRI_KS : 1; };
             for (int t = 1; t < nsb_max; ++t) {
                 for (int phase = 0; phase < 2; ++phase) {
                     const int tb = int(tiles.size());
+                    const int gb = int(groups.size());
                     int64_t toff = 0;
                     for (int f : plan.level_fronts[h]) {
                         const FrontDev& fr = plan.fronts[f];
@@ -1710,36 +1775,78 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                         if (t >= nsb) continue;
                         {   // lower, super-block row i = t
                             const int r0 = t * TRI_SB, r1 = std::min(nf, r0 + TRI_SB), m = r1 - r0, w = r0;
+                            const int ns = nsplit(w);
                             const int64_t tcur = toff;
-                            toff += int64_t(m) * w;
-                            if (phase == 0)   // T = L[Ri, 0:r0] * X[0:r0, 0:r0]   (m x w)
-                                emit(TriTask{fr.off + r0, fr.off, tcur, F, F, m, m, w, w, OP_DENSE, OP_LOWER_UNIT,
-                                             0, 0, 1, 1.f});
-                            else              // X[Ri, 0:r0] = -Linv_ii * T
+                            toff += int64_t(m) * w * ns;
+                            if (phase == 0) {   // T = L[Ri, 0:r0] * X[0:r0, 0:r0]   (m x w), split along K
+                                for (int sp = 0; sp < ns; ++sp) {
+                                    TriTask tk{fr.off + r0, fr.off, tcur + int64_t(sp) * m * w, F, F, m, m, w, w,
+                                               OP_DENSE, OP_LOWER_UNIT, 0, 0, 1, 1.f};
+                                    tk.k0 = sp * TRI_KS;
+                                    tk.k1 = ns > 1 ? std::min(w, (sp + 1) * TRI_KS) : w;
+                                    emit(tk);
+                                }
+                                if (ns > 1) groups.push_back(SplitGroup{tcur, int64_t(m) * w, ns});
+                            } else {            // X[Ri, 0:r0] = -Linv_ii * T
                                 emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + r0, F, m, F, m, w, m,
                                              OP_LOWER_UNIT, OP_DENSE, 0, 1, 0, -1.f});
+                            }
                         }
                         {   // upper, super-block row i = nsb - 1 - t
                             const int i = nsb - 1 - t;
                             const int r0 = i * TRI_SB, r1 = r0 + TRI_SB, m = r1 - r0, w = nf - r1;
+                            const int ns = nsplit(w);
                             const int64_t tcur = toff;
-                            toff += int64_t(m) * w;
-                            if (phase == 0)   // T = U[Ri, r1:nf] * Y[r1:nf, r1:nf]   (m x w)
-                                emit(TriTask{fr.off + int64_t(r1) * F + r0, fr.off + int64_t(r1) * F + r1, tcur,
-                                             F, F, m, m, w, w, OP_DENSE, OP_UPPER, 0, 0, 1, 1.f});
-                            else              // Y[Ri, r1:nf] = -Uinv_ii * T
+                            toff += int64_t(m) * w * ns;
+                            if (phase == 0) {   // T = U[Ri, r1:nf] * Y[r1:nf, r1:nf]   (m x w), split along K
+                                for (int sp = 0; sp < ns; ++sp) {
+                                    TriTask tk{fr.off + int64_t(r1) * F + r0, fr.off + int64_t(r1) * F + r1,
+                                               tcur + int64_t(sp) * m * w, F, F, m, m, w, w, OP_DENSE, OP_UPPER,
+                                               0, 0, 1, 1.f};
+                                    tk.k0 = sp * TRI_KS;
+                                    tk.k1 = ns > 1 ? std::min(w, (sp + 1) * TRI_KS) : w;
+                                    emit(tk);
+                                }
+                                if (ns > 1) groups.push_back(SplitGroup{tcur, int64_t(m) * w, ns});
+                            } else {            // Y[Ri, r1:nf] = -Uinv_ii * T
                                 emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + int64_t(r1) * F + r0,
                                              F, m, F, m, w, m, OP_UPPER, OP_DENSE, 0, 1, 0, -1.f});
+                            }
                         }
                     }
                     tmax = std::max(tmax, toff);
                     lv.push_back({tb, int(tiles.size())});
+                    if (int(groups.size()) > gb) lv.push_back({-1 - gb, -1 - int(groups.size())});   // split-K reduce
                 }
             }
             lu.tri_ranges.push_back(lv);
+            // G = L21 * Linv11 and H = Uinv11 * U12 (FP32 factors) into the G/H scratch
+            std::vector<std::pair<int, int>> gv;
+            if (lu.gh) {
+                for (int which = 0; which < 2; ++which) {
+                    const int tb = int(tiles.size());
+                    int64_t goff = 0;
+                    for (int f : plan.level_fronts[h]) {
+                        const FrontDev& fr = plan.fronts[f];
+                        const int nf = fr.nf, nb = fr.nb, F = fr.F;
+                        const int64_t cur = goff;
+                        goff += int64_t(nf) * nb;
+                        if (nf == 0 || nb == 0) continue;
+                        if (which == 0)   // G (nb x nf)
+                            emit(TriTask{fr.off + nf, fr.off, cur, F, F, nb, nb, nf, nf, OP_DENSE, OP_LOWER_UNIT,
+                                         0, 0, 1, 1.f});
+                        else              // H (nf x nb)
+                            emit(TriTask{fr.off, fr.off + int64_t(nf) * F, cur, F, F, nf, nf, nb, nf, OP_UPPER,
+                                         OP_DENSE, 0, 0, 1, 1.f});
+                    }
+                    gv.push_back({tb, int(tiles.size())});
+                }
+            }
+            lu.gh_ranges.push_back(gv);
         }
         lu.d_tri_tasks = upload(lu, tasks, s);
         lu.d_tri_tiles = upload(lu, tiles, s);
+        lu.d_tri_groups = upload(lu, groups, s);
         lu.d_tri_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax, 1)));
         lu.tri_flops = 0.0;
         for (const TriTask& t : tasks) lu.tri_flops += double(t.M) * t.N * t.K;   // ~ half are structural zeros
@@ -1837,7 +1944,7 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
             const int pend = std::min(P0 + OB, maxnf);
             for (int p = P0; p < pend; p += B) {
                 cudaEvent_t ev_pn = lu.timer ? lu.timer->start(s) : nullptr;
-                k_panel_diag<T, B><<<nfr, NT, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert); IEMIC_COUNT_LAUNCH();
+                k_panel_diag<T, B><<<nfr, 32, 0, s>>>(lu.d_fronts, lf, p, front, dinv, lu.d_piv, tau, lu.d_npert); IEMIC_COUNT_LAUNCH();
                 dim3 g1((maxF + NT - 1) / NT, nfr);
                 k_rowperm_u12<T, B><<<g1, NT, 0, s>>>(lu.d_fronts, lf, p, P0, front, dinv, lu.d_piv); IEMIC_COUNT_LAUNCH();
                 dim3 g3((maxF - p + NT - 1) / NT, nfr);
@@ -1869,12 +1976,24 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
         const int maxblk = (maxnf + B - 1) / B;
         cudaEvent_t ev_inv = lu.timer ? lu.timer->start(s) : nullptr;
         k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
-        for (const auto& rg : lu.tri_ranges[h]) {
-            if (rg.second > rg.first)
-                k_tri_gemm<T><<<rg.second - rg.first, 256, 0, s>>>(
-                    static_cast<const TriTask*>(lu.d_tri_tasks), static_cast<const TriTile*>(lu.d_tri_tiles) + rg.first,
-                    front, static_cast<T*>(lu.d_tri_scratch)); IEMIC_COUNT_LAUNCH();
-        }
+        auto task_launch = [&](const std::pair<int, int>& rg, T* scr) {
+            if (rg.first < 0) {   // split-K reduce of groups [-1-first, -1-second)
+                const int g0 = -1 - rg.first, g1 = -1 - rg.second;
+                k_split_reduce<T><<<dim3(64, std::min(g1 - g0, 65535)), 256, 0, s>>>(
+                    static_cast<const SplitGroup*>(lu.d_tri_groups) + g0, g1 - g0, scr); IEMIC_COUNT_LAUNCH();
+                return;
+            }
+            if (rg.second <= rg.first) return;
+            const TriTask* tk = static_cast<const TriTask*>(lu.d_tri_tasks);
+            const TriTile* tl = static_cast<const TriTile*>(lu.d_tri_tiles) + rg.first;
+            if constexpr (sizeof(T) == 4)
+                k_task_gemm_f32<<<rg.second - rg.first, 256, FG_SMEM, s>>>(tk, tl, reinterpret_cast<float*>(front),
+                                                                           reinterpret_cast<float*>(scr));
+            else
+                k_tri_gemm<T><<<rg.second - rg.first, 256, 0, s>>>(tk, tl, front, scr);
+            IEMIC_COUNT_LAUNCH();
+        };
+        for (const auto& rg : lu.tri_ranges[h]) task_launch(rg, static_cast<T*>(lu.d_tri_scratch));
         if (lu.gh) {
             const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
             int64_t mt = 0, mnb = 0;
@@ -1884,9 +2003,9 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
                 mnb = std::max<int64_t>(mnb, int64_t(fr.nf) * fr.nb);
             }
             if (mt > 0) {
-                k_gh<T, false><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+                task_launch(lu.gh_ranges[h][0], scratch);
                 k_gh_copy<T, false><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-                k_gh<T, true><<<dim3(int(mt), nfr), 256, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
+                task_launch(lu.gh_ranges[h][1], scratch);
                 k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
             }
         }

@@ -87,8 +87,9 @@ struct NdLu {
     std::vector<int> tgroup_start[4];
     // recursive triangular inversion: tasks, tiles, per level the tile ranges
     // of its launches, and the scratch of the first product of each merge
-    void *d_tri_tasks = nullptr, *d_tri_tiles = nullptr, *d_tri_scratch = nullptr;
+    void *d_tri_tasks = nullptr, *d_tri_tiles = nullptr, *d_tri_scratch = nullptr, *d_tri_groups = nullptr;
     std::vector<std::vector<std::pair<int, int>>> tri_ranges;
+    std::vector<std::vector<std::pair<int, int>>> gh_ranges;   // per level: G tiles, H tiles (FP32 factors)
     double tri_flops = 0.0;
     void* d_scratch = nullptr;
     cudaGraphExec_t sweep_exec = nullptr; // captured forward + backward level sweeps
