@@ -1855,13 +1855,15 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     ck(cudaStreamSynchronize(s));
 }
 
-// Ruiz equilibration (FP64) of the wet block of J
+// Ruiz equilibration (FP64) of the wet block of J: each sweep divides rows and
+// then columns by the square roots of their largest magnitudes
+constexpr int kRuizSweeps = 8;
 static void equilibrate(NdLu& lu, const int* rp, const int* ci, const double* val, cudaStream_t s) {
     const NdPlan& P = *lu.plan;
     const int nd = P.ndim, G = blocks_for(nd);
     k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dr); IEMIC_COUNT_LAUNCH();
     k_fill<<<G, NT, 0, s>>>(nd, 1.0, lu.d_dc); IEMIC_COUNT_LAUNCH();
-    for (int it = 0; it < 3; ++it) {
+    for (int it = 0; it < kRuizSweeps; ++it) {
         k_rowmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dc, lu.d_dr); IEMIC_COUNT_LAUNCH();
         ck(cudaMemsetAsync(lu.d_cmax, 0, sizeof(double) * nd, s));
         k_colmax<<<G, NT, 0, s>>>(nd, lu.d_g2r, rp, ci, val, lu.d_dr, lu.d_dc, lu.d_cmax); IEMIC_COUNT_LAUNCH();
