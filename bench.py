@@ -85,24 +85,26 @@ def dist_init():
     return rank, world
 
 
-def barrier_max(value, world):
+def _all_reduce(value, world, op_name):
+    """Replica aggregation over the process group (NCCL on GPUs, gloo on CPU)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=getattr(dist.ReduceOp, op_name))
     return float(t.item())
+
+
+def barrier_max(value, world):
+    """Max over ranks: the timed region ends when the slowest replica ends."""
+    return _all_reduce(value, world, "MAX")
 
 
 def barrier_sum(value, world):
-    if world == 1:
-        return value
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    """Sum over ranks: the work all replicas did."""
+    return _all_reduce(value, world, "SUM")
 
 
 class Clocks:

@@ -811,13 +811,6 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
 //   stages per level and sweep, because on GB300's FP64 pipe forming G and H
 //   costs more than the few extra launches of their handful of solves.
 // ---------------------------------------------------------------------------
-enum { MD_DENSE = 0, MD_LOWER_UNIT = 1, MD_UPPER = 2 };
-template <class T, int MODE>
-__device__ __forceinline__ T opld(const T* A, int F, int r, int c) {
-    if (MODE == MD_DENSE) return A[int64_t(c) * F + r];
-    if (MODE == MD_LOWER_UNIT) return r > c ? A[int64_t(c) * F + r] : (r == c ? T(1) : T(0));
-    return r <= c ? A[int64_t(c) * F + r] : T(0);
-}
 
 // write the inverted diagonal blocks (Linv_jj strict lower, Uinv_jj upper)
 template <class T, int B>

@@ -131,3 +131,56 @@ def test_adjoint_bad_arguments():
         g.adjointPsiM(x, sector=(5, 2))
     with pytest.raises(IemicError):
         g.adjointPsiM(x, pars=(99,))
+
+
+def _sector_g(g, x, sector):
+    """max psi_M over the sector [i0, i1) through iemic_psim_max_grad_dev."""
+    import torch
+    xd = _dev(x)
+    grad = torch.zeros(g.ndim, dtype=torch.float64, device="cuda")
+    gv = ctypes.c_double()
+    jk = (ctypes.c_int * 2)()
+    rc = g.L.iemic_psim_max_grad_dev(g.handle, ctypes.c_void_p(xd.data_ptr()), sector[0], sector[1],
+                                     ctypes.byref(gv), jk, ctypes.c_void_p(grad.data_ptr()))
+    assert rc == 0
+    return gv.value
+
+
+def test_adjoint_global_sector_20_cells():
+    """Gradient of the sector-restricted max overturning of a periodic global
+    ocean (24x12x6, seeded land) w.r.t. the injected surface freshwater flux,
+    checked by central differences on 20 seeded cells."""
+    from iemic import workloads as W
+    cfg, lm, _ = global_case()
+    cfg = dict(cfg, its=2, ite=2)            # injected T/S forcing fields
+    n, m = cfg["n"], cfg["m"]
+    lat = np.linspace(-1, 1, m)[:, None] * np.ones((1, n))
+    frc = dict(tatm=np.cos(np.pi * lat / 2).ravel(), emip=(0.5 * np.sin(np.pi * lat)).ravel())
+    g = make_gpu(cfg, lm, frc)
+    g.setPar("Combined Forcing", 0.05)
+    x, st = g.newton(np.zeros(g.ndim), precision=0, max_iters=25, tol=1e-10)
+    assert st["status"] == 0, st
+    sector = (6, 18)
+    gval, fields, _, ast = g.adjointPsiM(x, sector=sector, precision=1)
+    assert ast["status"] == 0
+    assert gval == pytest.approx(_sector_g(g, x, sector), rel=1e-13)
+    ge = fields["emip"]
+    emip0 = frc["emip"].reshape(m, n)
+    landm = g.getLandMask().reshape(cfg["l"] + 2, m + 2, n + 2)
+    ocean = np.argwhere(landm[cfg["l"], 1:m + 1, 1:n + 1] == 0)
+    cells = ocean[np.random.default_rng(20).choice(len(ocean), 20, replace=False)]
+    h = 1e-4
+    scale = np.abs(ge).max()
+    assert scale > 0
+    for j, i in cells:
+        vals = []
+        for sgn in (1, -1):
+            f = emip0.copy()
+            f[j, i] += sgn * h
+            g.setForcing(emip=f.ravel())
+            xs, st = g.newton(x, precision=0, max_iters=20, tol=1e-10)
+            assert st["status"] == 0, st
+            vals.append(_sector_g(g, xs, sector))
+        g.setForcing(emip=emip0.ravel())
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - ge[j, i]) <= 1e-5 * scale, (j, i, fd, ge[j, i], scale)
