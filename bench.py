@@ -330,14 +330,16 @@ def run_ours(args, rank, world):
             results[label].update(launches=launches, clocks=clk)
 
     # --- per-kernel device times: the timed mixed steps repeated from the same
-    # point with CUDA events around every launch (eager launches, on the stream
-    # the kernels run on), so the timed region above stays uninstrumented
+    # point with CUDA events around every launch (event nodes in the same
+    # captured graphs, on the stream the kernels run on), so the timed region
+    # above stays uninstrumented
     x = x_start.clone()
     oc.setPar("Salinity Forcing", par_w)
     oc.kernelTiming(True)
     cont_dev(x, 1, args.steps)
     torch.cuda.synchronize()
     results["mixed"]["kstats"] = oc.kernelStats()
+    results["mixed"]["timing_failures"] = oc.kernelTimingFailures()
     oc.kernelTiming(False)
 
     # --- end to end through the public API with host buffers (mixed path)
@@ -405,7 +407,7 @@ def run_newton1(args):
     out = {"mode": "newton1", "workload": args.workload, "solver": oc.solverInfo()}
     for label, prec in (("mixed", 1), ("fp64", 0)):
         # pass 0 builds the plan and allocates; pass 1 times every kernel class
-        # (eager launches); pass 2 runs as in production (graph-launched sweeps)
+        # (the same graphs with event nodes); pass 2 runs untimed, as in production
         for rep in range(3):
             oc.kernelTiming(rep == 1)
             t0 = time.perf_counter()
@@ -419,9 +421,10 @@ def run_newton1(args):
             wall = time.perf_counter() - t0
             if rep == 1:
                 ks = oc.kernelStats()
+                failed = oc.kernelTimingFailures()
                 timed = {"wall_s": wall, "solve1": s1, "solve2": s2}
             oc.kernelTiming(False)
-        out[label] = {"wall_s": wall, "solve1": s1, "solve2": s2, "timed_pass": timed,
+        out[label] = {"wall_s": wall, "solve1": s1, "solve2": s2, "timed_pass": timed, "timing_failures": failed,
                       "classes_ms": {k: round(v["ms"], 3) for k, v in ks.items()},
                       "launches": {k: v["launches"] for k, v in ks.items()}}
     print(json.dumps(out), flush=True)

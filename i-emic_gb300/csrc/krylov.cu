@@ -364,6 +364,7 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
             reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0); IEMIC_COUNT_LAUNCH();
             ck(cudaMemcpyAsync(K.hpin, K.h, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, s));
             ck(cudaStreamSynchronize(s));
+            e.timer.drain();   // before the next replay re-records the graph's timing events
             const double hn = std::sqrt(K.hpin[j + 1]);
             if (!std::isfinite(hn)) throw EngineError(IEMIC_ERR_NAN);
             if (hn > 0.0) {
@@ -400,6 +401,7 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
         precond(lu, e, w, z, transpose, s);
         add_to<T><<<G, 256, 0, s>>>(n, z, x); IEMIC_COUNT_LAUNCH();
         ck(cudaStreamSynchronize(s));   // y is a host temporary
+        e.timer.drain();
     }
     ck(cudaGetLastError());
     *relres_out = relres;

@@ -1521,6 +1521,13 @@ int blocks_for(int64_t work, int per = NT) {
 NdLu::~NdLu() {
     if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
     if (factor_exec) cudaGraphExecDestroy(factor_exec);
+    if (sweep_exec_timed) cudaGraphExecDestroy(sweep_exec_timed);
+    if (factor_exec_timed) cudaGraphExecDestroy(factor_exec_timed);
+    for (auto* t : {&factor_tmpl, &sweep_tmpl})
+        for (const KTimer::Rec& r : *t) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
     for (void* p : allocs) cudaFree(p);
 }
 
@@ -2012,10 +2019,40 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
 // do not move (the CSR arrays of the engine and the factor storage), so it is
 // captured once into a CUDA graph and replayed; with kernel timing on it runs
 // eagerly so that every launch can be timed.
+// Capture `body` into a graph whose launches are timed by event nodes
+// (records into `tmpl`), once, then replay it and queue its records.
+template <class F>
+static void timed_graph(NdLu& lu, cudaGraphExec_t& exec, std::vector<KTimer::Rec>& tmpl, long long& nlaunch,
+                        cudaStream_t s, F body) {
+    if (!exec) {
+        cudaGraph_t g = nullptr;
+        ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const long long n0 = launch_counter();
+        lu.timer->sink = &tmpl;
+        body();
+        lu.timer->sink = nullptr;
+        nlaunch = launch_counter() - n0;
+        launch_counter() = n0;
+        ck(cudaStreamEndCapture(s, &g));
+        const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        ck(e);
+    }
+    ck(cudaGraphLaunch(exec, s));
+    launch_counter() += nlaunch;
+    lu.timer->replayed(tmpl);
+}
+
 template <class T, int B>
 static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {
     if (lu.timer && lu.timer->on) {
-        factor_body<T, B>(lu, rp, ci, values, s);
+        if (lu.factor_exec_timed && (lu.fg_rp != rp || lu.fg_ci != ci || lu.fg_val != values))
+            throw EngineError(IEMIC_ERR_STATE);
+        lu.fg_rp = rp;
+        lu.fg_ci = ci;
+        lu.fg_val = values;
+        timed_graph(lu, lu.factor_exec_timed, lu.factor_tmpl, lu.factor_launches_timed, s,
+                    [&] { factor_body<T, B>(lu, rp, ci, values, s); });
     } else {
         if (lu.factor_exec && (lu.fg_rp != rp || lu.fg_ci != ci || lu.fg_val != values)) {
             cudaGraphExecDestroy(lu.factor_exec);
@@ -2150,7 +2187,8 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
     if (kt && kt->on) {
-        sweeps_t<T, B>(lu, s);   // eager, so every launch can be timed
+        timed_graph(lu, lu.sweep_exec_timed, lu.sweep_tmpl, lu.sweep_launches_timed, s,
+                    [&] { sweeps_t<T, B>(lu, s); });
     } else {
         if (!lu.sweep_exec) {
             cudaGraph_t g = nullptr;

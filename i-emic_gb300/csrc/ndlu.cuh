@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <vector>
 
+#include "ktimer.cuh"
+
 namespace iemic {
 
 // One frontal matrix of the elimination tree: `nf` own ("fully summed")
@@ -46,8 +48,6 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
                    const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel);
 
 // Device-resident factorisation for one precision.
-struct KTimer;
-
 struct NdLu {
     int prec = 0;   // 0 FP64, 1 FP32
     const NdPlan* plan = nullptr;
@@ -94,6 +94,10 @@ struct NdLu {
     void* d_scratch = nullptr;
     cudaGraphExec_t sweep_exec = nullptr; // captured forward + backward level sweeps
     cudaGraphExec_t factor_exec = nullptr;  // captured factorisation
+    // the same graphs with timing event nodes (kernel timing on)
+    cudaGraphExec_t factor_exec_timed = nullptr, sweep_exec_timed = nullptr;
+    std::vector<KTimer::Rec> factor_tmpl, sweep_tmpl;
+    long long factor_launches_timed = 0, sweep_launches_timed = 0;
     long long factor_launches = 0;
     const void *fg_rp = nullptr, *fg_ci = nullptr, *fg_val = nullptr;   // arrays the factor graph reads
     long long sweep_launches = 0;           // kernels in the captured sweeps

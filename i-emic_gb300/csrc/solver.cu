@@ -145,6 +145,8 @@ int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out) 
     GUARD_END
 }
 
+long long iemic_kernel_timing_failures(iemic_ocean* h) { return h ? h->e.timer.failed : -1; }
+
 int iemic_get_stream(iemic_ocean* h, void** stream) {
     if (!h || !stream) return IEMIC_ERR_ARG;
     *stream = static_cast<void*>(h->e.stream);

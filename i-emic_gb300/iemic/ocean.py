@@ -176,6 +176,7 @@ SIGNATURES = {
     "iemic_continuation_run_dev": [_VP, _VP, ctypes.POINTER(ContinuationOpts),
                                    ctypes.POINTER(ContinuationStats)],
     "iemic_launch_count": [],
+    "iemic_kernel_timing_failures": [_VP],
 }
 _VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts",
                 "iemic_default_adjoint_opts"}
@@ -197,7 +198,7 @@ def load_library(path=None, build_if_missing=True):
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = None if name in _VOID_RETURN else ctypes.c_int
-        if name == "iemic_launch_count":
+        if name in ("iemic_launch_count", "iemic_kernel_timing_failures"):
             fn.restype = ctypes.c_longlong
     if path == _build.LIB:
         _lib = L
@@ -453,6 +454,10 @@ class Ocean:
             self._check(self.L.iemic_kernel_stats_get(self._h, k, ctypes.byref(st)), "kernelStats")
             out[name] = _asdict(st)
         return out
+
+    def kernelTimingFailures(self):
+        """Timing records the runtime could not time (0 when every launch was timed)."""
+        return int(self.L.iemic_kernel_timing_failures(self._h))
 
     def stream(self):
         """The cudaStream_t (as an int) all calls on this handle run on."""

@@ -283,6 +283,8 @@ typedef struct {
 } iemic_kernel_stats;
 int iemic_kernel_timing(iemic_ocean* h, int enable);
 int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out);
+/* Timing records the runtime could not time since timing was enabled. */
+long long iemic_kernel_timing_failures(iemic_ocean* h);
 /* Kernel launches this library has made in the process so far. */
 long long iemic_launch_count(void);
 /* The CUDA stream (cudaStream_t) every call on this handle runs on. */

@@ -90,3 +90,23 @@ def test_zero_rhs_and_bad_arguments():
         g.solve(-F, precision=7)
     with pytest.raises(IemicError):
         g.solve(-F, precision=0, restart=0)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_kernel_timing_through_graphs(prec):
+    """Timing on replays the same graphs with event nodes: same solution bits, every launch timed."""
+    g, o, M, x, F, pins = _setup("glob24")
+    sol0, st0 = g.solve(-F, precision=prec)
+    g.kernelTiming(True)
+    g.computeJacobian(x)                             # same J again: the next solve refactors
+    sol1, st1 = g.solve(-F, precision=prec)          # captured with timing nodes
+    assert st1["factorizations"] == 1, st1
+    sol2, st2 = g.solve(-F, precision=prec, reuse_preconditioner=1)
+    ks = g.kernelStats()
+    assert g.kernelTimingFailures() == 0
+    g.kernelTiming(False)
+    assert np.array_equal(sol0, sol1) and st0["iters"] == st1["iters"], (st0, st1)
+    assert np.array_equal(sol1, sol2)
+    fac = [ks[c] for c in ("factor_gemm", "factor_panel", "factor_inverse", "factor_setup")]
+    assert sum(k["launches"] for k in fac) > 0 and sum(k["ms"] for k in fac) > 0, ks
+    assert ks["solve_gemv"]["launches"] > 0 and ks["solve_gemv"]["ms"] > 0, ks
