@@ -74,6 +74,14 @@ struct KTimer {
     // after a replay of a graph captured with `sink = &tmpl`
     void replayed(const std::vector<Rec>& tmpl) { pending.insert(pending.end(), tmpl.begin(), tmpl.end()); }
     long long failed = 0;   // records whose elapsed time the runtime refused
+    // per-launch trace in completion order (class, device ms, algorithmic bytes)
+    struct Trace {
+        int cls;
+        float ms;
+        double bytes;
+    };
+    static constexpr size_t kTraceCap = size_t(1) << 20;
+    std::vector<Trace> trace;
     void drain() {
         for (const Rec& r : pending) {
             float t = 0.f;
@@ -83,6 +91,7 @@ struct KTimer {
                 ++failed;
                 t = 0.f;
             }
+            if (trace.size() < kTraceCap) trace.push_back({r.cls, t, r.bytes});
             ms[r.cls] += t;
             bytes[r.cls] += r.bytes;
             flops[r.cls] += r.flops;
@@ -97,6 +106,7 @@ struct KTimer {
     void reset() {
         drain();
         failed = 0;
+        trace.clear();
         for (int c = 0; c < IEMIC_KC_COUNT; ++c) ms[c] = bytes[c] = flops[c] = 0.0, launches[c] = 0;
     }
     ~KTimer() {

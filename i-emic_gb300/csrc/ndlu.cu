@@ -237,6 +237,23 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
         fr.parent = nodes[f].parent;
     }
     plan.nred = int(plan.r2g.size());
+    // couplings of the reduced rows to identity (dry, unpinned) unknowns, in
+    // CSR order: the right-hand side reduction subtracts only these
+    {
+        std::vector<char> ident(ndim, 0);
+        for (int r : plan.dry_rows) ident[r] = 1;
+        for (int p : plan.pins) ident[p] = 0;
+        plan.dry_ptr.assign(1, 0);
+        for (int q = 0; q < plan.nred; ++q) {
+            const int g = plan.r2g[q];
+            for (int e = row_ptr[g]; e < row_ptr[g + 1]; ++e)
+                if (ident[col_idx[e]]) {
+                    plan.dry_e.push_back(e);
+                    plan.dry_c.push_back(col_idx[e]);
+                }
+            plan.dry_ptr.push_back(int(plan.dry_e.size()));
+        }
+    }
 
     // 6. boundary unknowns: the non-deferred unknowns of the ring of columns
     //    around the subtree region, plus the deferred surface pressures of the
@@ -1065,16 +1082,14 @@ __global__ void k_gh_copy(const FrontDev* __restrict__ fronts, const int* __rest
 // (the solve phase works in FP64 for both factor precisions: FP32 factors are
 // read and upcast, so the accumulation error is FP64's, not FP32's)
 template <class TV>
-__global__ void k_reduce_rhs(int nred, const int* __restrict__ r2g, const char* __restrict__ isdry,
-                             const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ val,
-                             const double* __restrict__ dr, const TV* __restrict__ r, double* __restrict__ red) {
+__global__ void k_reduce_rhs(int nred, const int* __restrict__ r2g, const int* __restrict__ dry_ptr,
+                             const int* __restrict__ dry_e, const int* __restrict__ dry_c,
+                             const double* __restrict__ val, const double* __restrict__ dr, const TV* __restrict__ r,
+                             double* __restrict__ red) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nred; q += gridDim.x * blockDim.x) {
         const int g = r2g[q];
         double s = double(r[g]);
-        for (int e = rp[g]; e < rp[g + 1]; ++e) {
-            int c = ci[e];
-            if (isdry[c] == 1) s -= val[e] * double(r[c]);
-        }
+        for (int k = dry_ptr[q]; k < dry_ptr[q + 1]; ++k) s -= val[dry_e[k]] * double(r[dry_c[k]]);
         red[q] = dr[g] * s;
     }
 }
@@ -1105,7 +1120,11 @@ __global__ void k_expand(int ndim, const int* __restrict__ g2r, const char* __re
 struct WorkItem {
     int front, row0, col0, chunk, stage;
 };
-constexpr int GR = 256, GC = 256;
+// solve GEMV tiles: GT rows x GC columns per block of GR threads; the
+// block's threads form GR / GT column groups of GC * GT / GR columns each, so
+// a thread walks one row of one column group (a short dependent chain of
+// loads) and a tile's column groups are summed in shared memory
+constexpr int GR = 256, GC = 256, GT = 64, NCG = GR / GT, CGW = GC / NCG;
 enum { ST_LINV = 0, ST_UINV = 1, ST_L21 = 2, ST_U12 = 3, NSTAGE = 4 };
 // rows and columns of a stage's block inside a front
 __host__ __device__ inline void stage_block(int st, int nf, int F, int& r0, int& r1, int& c0, int& c1) {
@@ -1116,35 +1135,37 @@ __host__ __device__ inline void stage_block(int st, int nf, int F, int& r0, int&
 }
 
 // forward prologue: w = [red_C ; 0] + children's update vectors, then the
-// block-local row permutations applied to the own part (into wp)
+// block-local row permutations applied to the own part (into wp). A thread
+// per row: the inverse extend-add map gives each row its children's update
+// rows, added in slot order (the order of a scatter child by child).
+__device__ __forceinline__ double fwd_row(const FrontDev& fr, int q, const double* __restrict__ red,
+                                          const int2* __restrict__ einv, const double* __restrict__ u0,
+                                          const double* __restrict__ u1) {
+    double w = q < fr.nf ? red[fr.red0 + q] : 0.0;
+    const int2 a = einv[fr.woff + q];
+    if (a.x >= 0) w += u0[a.x];
+    if (a.y >= 0) w += u1[a.y];
+    return w;
+}
 __global__ void __launch_bounds__(NT) k_fwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                                   const int* __restrict__ child_of, const int* __restrict__ emap,
+                                                   const int* __restrict__ child_of, const int2* __restrict__ einv,
                                                    const int* __restrict__ piv, const double* __restrict__ red,
                                                    double* __restrict__ W, double* __restrict__ WP, int B) {
-    const int f = lf[blockIdx.x];
+    const int f = lf[blockIdx.y];
     const FrontDev fr = fronts[f];
-    const int F = fr.F, nf = fr.nf, tid = threadIdx.x;
-    double* w = W + fr.woff;
-    for (int q = tid; q < F; q += NT) w[q] = q < nf ? red[fr.red0 + q] : 0.0;
-    __syncthreads();
-    for (int s = 0; s < 2; ++s) {
-        int c = child_of[2 * f + s];
-        if (c < 0) continue;
-        const FrontDev ch = fronts[c];
-        const double* u = WP + ch.woff + ch.nf;   // child's update vector
-        const int* em = emap + ch.emap_off;
-        for (int a = tid; a < ch.nb; a += NT) w[em[a]] += u[a];
-        __syncthreads();
-    }
-    double* wp = WP + fr.woff;
-    for (int q = tid; q < F; q += NT) {
-        if (q < nf) {
-            int p = (q / B) * B;
-            wp[q] = w[p + piv[fr.red0 + q]];
-        } else {
-            wp[q] = w[q];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.F) return;
+    const double* u[2] = {nullptr, nullptr};
+    for (int sl = 0; sl < 2; ++sl) {
+        const int c = child_of[2 * f + sl];
+        if (c >= 0) {
+            const FrontDev ch = fronts[c];
+            u[sl] = WP + ch.woff + ch.nf;   // child's update vector
         }
     }
+    const double wq = fwd_row(fr, q, red, einv, u[0], u[1]);
+    W[fr.woff + q] = wq;
+    WP[fr.woff + q] = q < fr.nf ? fwd_row(fr, (q / B) * B + piv[fr.red0 + q], red, einv, u[0], u[1]) : wq;
 }
 // Compensated (double-float) accumulation of a * (xh + xl) into (s, c) with
 // FP32 instructions only: the product's rounding error comes from an FMA and
@@ -1163,10 +1184,11 @@ __device__ __forceinline__ void dd_acc(float& s, float& c, float a, float xh, fl
     c = __fadd_rn(c, __fadd_rn(err, e));
 }
 
-// Partial GEMV products of one stage: thread per row of a (GR-row, GC-column)
-// tile; ST_LINV uses the strict lower part plus the unit diagonal, ST_UINV the
+// Partial GEMV products of one stage over a (GT-row, GC-column) tile;
+// ST_LINV uses the strict lower part plus the unit diagonal, ST_UINV the
 // upper part, ST_L21 and ST_U12 the dense blocks with a minus sign. Partial
-// sums go to part[off + chunk * rows + (r - r0)].
+// sums go to part[off + chunk * rows + (r - r0)], the column groups of a tile
+// added in order.
 struct StageBufs {
     double* part[4];
     const int64_t* off[4];
@@ -1179,9 +1201,11 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
     const int F = fr.F, nf = fr.nf;
     int br0, br1, bc0, bc1;
     stage_block(ST, nf, F, br0, br1, bc0, bc1);
-    const int r = it.row0 + threadIdx.x;
+    const int rl = threadIdx.x % GT, cg = threadIdx.x / GT;
+    const int r = it.row0 + rl;
     __shared__ double xs[GC];
     __shared__ float2 xs2[GC];
+    __shared__ double gsum[NCG - 1][GT];
     const double* x = X + fr.woff;
     for (int q = threadIdx.x; q < GC; q += GR) {
         const double v = it.col0 + q < bc1 ? x[it.col0 + q] : 0.0;
@@ -1193,17 +1217,13 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
         }
     }
     __syncthreads();
-    if (r >= br1) return;
+    const bool live = r < br1;
     const T* A = front + fr.off + r;
-    const int cend = min(bc1, it.col0 + GC);
-    int c0 = it.col0, c1 = cend;
-    bool diag = false;
-    if (ST == ST_LINV) {
-        c1 = min(cend, r);
-        diag = r >= it.col0 && r < cend;
-    } else if (ST == ST_UINV) {
-        c0 = max(it.col0, r);
-    }
+    const int g0 = it.col0 + cg * CGW;
+    int c0 = g0, c1 = min(bc1, g0 + CGW);
+    if (ST == ST_LINV) c1 = min(c1, r);
+    else if (ST == ST_UINV) c0 = max(c0, r);
+    if (!live) c1 = c0;
     const float sg = (ST == ST_L21 || ST == ST_U12) ? -1.f : 1.f;
     double out;
     if (sizeof(T) == 4) {
@@ -1226,14 +1246,18 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
             dd_acc(sh, sl, sg * float(A[int64_t(c) * F]), xv.x, xv.y);
         }
         out = double(sh) + double(sl);
-        if (diag) out += xs2[r - it.col0].x + double(xs2[r - it.col0].y);
     } else {
         double acc = 0.0;
 #pragma unroll 4
         for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * F]) * xs[c - it.col0];
         out = double(sg) * acc;
-        if (diag) out += xs[r - it.col0];
     }
+    if (cg > 0) gsum[cg - 1][rl] = out;
+    __syncthreads();
+    if (cg > 0 || !live) return;
+    for (int k = 0; k < NCG - 1; ++k) out += gsum[k][rl];
+    if (ST == ST_LINV && r >= it.col0 && r < min(bc1, it.col0 + GC))   // unit diagonal
+        out += sizeof(T) == 4 ? xs2[r - it.col0].x + double(xs2[r - it.col0].y) : xs[r - it.col0];
     part[part_off[it.front] + int64_t(it.chunk) * (br1 - br0) + (r - br0)] = out;
 }
 template <class T>
@@ -1588,6 +1612,26 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     for (int r : plan.dry_rows) isdry[r] = 1;
     for (int r : plan.pins) isdry[r] = 2;
     lu.d_isdry = upload(lu, isdry, s);
+    lu.d_dry_ptr = upload(lu, plan.dry_ptr, s);
+    lu.d_dry_e = upload(lu, plan.dry_e, s);
+    lu.d_dry_c = upload(lu, plan.dry_c, s);
+    // inverse extend-add maps: for each row of a front's solve vector, the
+    // update-vector row of the child in slot 0 (.x) and slot 1 (.y), or -1
+    {
+        std::vector<int2> einv(size_t(std::max<int64_t>(plan.w_entries, 1)), make_int2(-1, -1));
+        for (int f = 0; f < plan.nfronts; ++f) {
+            const FrontDev& ch = plan.fronts[f];
+            if (ch.parent < 0) continue;
+            const FrontDev& pa = plan.fronts[ch.parent];
+            for (int a = 0; a < ch.nb; ++a) {
+                const int q = plan.emap[ch.emap_off + a];
+                int& slot = plan.child_slot[f] == 0 ? einv[pa.woff + q].x : einv[pa.woff + q].y;
+                if (q < 0 || q >= pa.F || slot != -1) throw EngineError(IEMIC_ERR_STATE);
+                slot = a;
+            }
+        }
+        lu.d_einv = upload(lu, einv, s);
+    }
     lu.d_asm_src = upload(lu, plan.asm_src, s);
     lu.d_asm_dst = upload(lu, plan.asm_dst, s);
     lu.d_asm_row = upload(lu, plan.asm_row, s);
@@ -1639,9 +1683,9 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                 int r0, r1, c0, c1;
                 stage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
                 for (int c = c0, ch = 0; c < c1; c += GC, ++ch)
-                    for (int r = r0; r < r1; r += GR) {
+                    for (int r = r0; r < r1; r += GT) {
                         // tiles holding no entry of a triangular part are skipped
-                        if (st == ST_LINV && r + GR <= fr.nf && c >= r + GR) continue;
+                        if (st == ST_LINV && r + GT <= fr.nf && c >= r + GT) continue;
                         if (st == ST_UINV && c + GC <= r) continue;
                         gitems[g].push_back(WorkItem{f, r, c, ch, st});
                     }
@@ -2143,7 +2187,8 @@ static void sweeps_t(NdLu& lu, cudaStream_t s) {
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         {
             cudaEvent_t ev = kt ? kt->start(s) : nullptr;
-            k_fwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
+            k_fwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of,
+                                                                                lu.d_einv, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
         if (lu.gh) {
@@ -2183,7 +2228,8 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
     KTimer* kt = lu.timer;
     {
         cudaEvent_t ev = kt ? kt->start(s) : nullptr;
-        k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_isdry, rp, ci, val, lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
+        k_reduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_dry_ptr, lu.d_dry_e, lu.d_dry_c, val,
+                                                            lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
     if (kt && kt->on) {

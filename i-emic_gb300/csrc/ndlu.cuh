@@ -36,6 +36,7 @@ struct NdPlan {
     std::vector<int> child_slot;    // slot of each front in its parent
     std::vector<int> dry_rows;      // unknowns the factorisation leaves out (identity rows, pins)
     std::vector<int> pins;          // pinned pressure unknowns
+    std::vector<int> dry_ptr, dry_e, dry_c;   // per reduced row: CSR entries (and columns) on identity unknowns
     std::vector<int> asm_src;       // CSR entry index
     std::vector<int> asm_row;       // its row
     std::vector<int64_t> asm_dst;   // offset in the front storage
@@ -60,6 +61,8 @@ struct NdLu {
     std::vector<int> child_start[2];
     int *d_vars = nullptr, *d_emap = nullptr, *d_r2g = nullptr, *d_g2r = nullptr, *d_child_of = nullptr;
     char* d_isdry = nullptr;                // 1 for unknowns left out of the factorisation
+    int *d_dry_ptr = nullptr, *d_dry_e = nullptr, *d_dry_c = nullptr;   // NdPlan::dry_*
+    int2* d_einv = nullptr;                 // per solve-vector row: child update rows (slot 0, slot 1) or -1
     int* d_asm_src = nullptr;
     int* d_asm_row = nullptr;
     double *d_dr = nullptr, *d_dc = nullptr, *d_cmax = nullptr;   // equilibration scalings

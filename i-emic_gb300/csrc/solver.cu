@@ -147,6 +147,22 @@ int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out) 
 
 long long iemic_kernel_timing_failures(iemic_ocean* h) { return h ? h->e.timer.failed : -1; }
 
+int iemic_kernel_trace(iemic_ocean* h, int cap, int* kclass, float* ms, double* bytes, int* count) {
+    if (!h || !count || cap < 0 || (cap > 0 && (!kclass || !ms || !bytes))) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    ck(cudaStreamSynchronize(h->e.stream));
+    h->e.timer.drain();
+    const auto& tr = h->e.timer.trace;
+    const int n = static_cast<int>(tr.size());
+    for (int i = 0; i < n && i < cap; ++i) {
+        kclass[i] = tr[i].cls;
+        ms[i] = tr[i].ms;
+        bytes[i] = tr[i].bytes;
+    }
+    *count = n;
+    GUARD_END
+}
+
 int iemic_get_stream(iemic_ocean* h, void** stream) {
     if (!h || !stream) return IEMIC_ERR_ARG;
     *stream = static_cast<void*>(h->e.stream);

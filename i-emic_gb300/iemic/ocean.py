@@ -177,6 +177,7 @@ SIGNATURES = {
                                    ctypes.POINTER(ContinuationStats)],
     "iemic_launch_count": [],
     "iemic_kernel_timing_failures": [_VP],
+    "iemic_kernel_trace": [_VP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float), _DP, _IP],
 }
 _VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts",
                 "iemic_default_adjoint_opts"}
@@ -454,6 +455,21 @@ class Ocean:
             self._check(self.L.iemic_kernel_stats_get(self._h, k, ctypes.byref(st)), "kernelStats")
             out[name] = _asdict(st)
         return out
+
+    def kernelTrace(self):
+        """Per-launch (class name, device ms, algorithmic bytes) since timing was enabled."""
+        cnt = ctypes.c_int(0)
+        self._check(self.L.iemic_kernel_trace(self._h, 0, None, None, None, ctypes.byref(cnt)), "kernelTrace")
+        n = cnt.value
+        cls = np.zeros(n, np.int32)
+        ms = np.zeros(n, np.float32)
+        nb = np.zeros(n, np.float64)
+        if n:
+            self._check(self.L.iemic_kernel_trace(self._h, n, cls.ctypes.data_as(_IP),
+                                                  ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                  nb.ctypes.data_as(_DP), ctypes.byref(cnt)), "kernelTrace")
+        names = {v: k for k, v in KERNEL_CLASSES.items()}
+        return [(names[int(c)], float(t), float(b)) for c, t, b in zip(cls, ms, nb)]
 
     def kernelTimingFailures(self):
         """Timing records the runtime could not time (0 when every launch was timed)."""

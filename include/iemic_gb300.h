@@ -285,6 +285,10 @@ int iemic_kernel_timing(iemic_ocean* h, int enable);
 int iemic_kernel_stats_get(iemic_ocean* h, int kclass, iemic_kernel_stats* out);
 /* Timing records the runtime could not time since timing was enabled. */
 long long iemic_kernel_timing_failures(iemic_ocean* h);
+/* Per-launch trace since timing was enabled, in completion order: kernel class,
+ * device time (ms) and algorithmic bytes of each timed launch. Copies up to
+ * `cap` entries; *count receives the number recorded (at most 2^20). */
+int iemic_kernel_trace(iemic_ocean* h, int cap, int* kclass, float* ms, double* bytes, int* count);
 /* Kernel launches this library has made in the process so far. */
 long long iemic_launch_count(void);
 /* The CUDA stream (cudaStream_t) every call on this handle runs on. */

@@ -103,7 +103,9 @@ def test_kernel_timing_through_graphs(prec):
     assert st1["factorizations"] == 1, st1
     sol2, st2 = g.solve(-F, precision=prec, reuse_preconditioner=1)
     ks = g.kernelStats()
+    tr = g.kernelTrace()
     assert g.kernelTimingFailures() == 0
+    assert len(tr) == sum(k["launches"] for k in ks.values())
     g.kernelTiming(False)
     assert np.array_equal(sol0, sol1) and st0["iters"] == st1["iters"], (st0, st1)
     assert np.array_equal(sol1, sol2)
