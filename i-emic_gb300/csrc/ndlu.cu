@@ -299,8 +299,9 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
         FrontDev& fr = plan.fronts[f];
         fr.nb = int(bvars[f].size());
         fr.F = fr.nf + fr.nb;
-        fr.off = off;
+        fr.lvl = nodes[f].height;
         off += int64_t(fr.F) * fr.F;
+        fr.foff = plan.factor_entries;   // before this front's entries are counted below
         fr.dinv_off = dinv;
         dinv += int64_t((fr.nf + panel - 1) / panel) * 2 * panel * panel;
         fr.voff = voff;
@@ -350,9 +351,34 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
             plan.level_maxnf[h] = std::max(plan.level_maxnf[h], plan.fronts[f].nf);
             plan.level_maxF[h] = std::max(plan.level_maxF[h], plan.fronts[f].F);
         }
+    // working offsets (per level, from 0) and contribution-ring offsets
+    int gap = 1;
+    for (int f = 0; f < NF; ++f)
+        if (plan.fronts[f].parent >= 0) gap = std::max(gap, plan.fronts[plan.fronts[f].parent].lvl - plan.fronts[f].lvl);
+    plan.contrib_ring = gap + 1;
+    plan.level_work.assign(H, 0);
+    std::vector<int64_t> level_contrib(H, 0);
+    for (int h = 0; h < H; ++h)
+        for (int f : plan.level_fronts[h]) {
+            FrontDev& fr = plan.fronts[f];
+            fr.off = plan.level_work[h];
+            plan.level_work[h] += int64_t(fr.F) * fr.F;
+            fr.soff = level_contrib[h];
+            level_contrib[h] += int64_t(fr.nb) * fr.nb;
+        }
+    for (int h = 0; h < H; ++h) {
+        plan.work_entries = std::max(plan.work_entries, plan.level_work[h]);
+        plan.contrib_slot_entries = std::max(plan.contrib_slot_entries, level_contrib[h]);
+    }
+    for (int f = 0; f < NF; ++f) plan.fronts[f].soff += (plan.fronts[f].lvl % plan.contrib_ring) * plan.contrib_slot_entries;
 
     // 9. assembly map: entry (r, c) goes to the front that eliminates the
-    //    earlier of its two unknowns
+    //    earlier of its two unknowns; entries grouped by level (each level
+    //    is assembled into the working area when its turn comes)
+    std::vector<int64_t> per_level(H, 0);
+    std::vector<int> ent_front;
+    std::vector<int> ent_q, ent_r;
+    std::vector<int64_t> ent_dst;
     for (int r = 0; r < ndim; ++r) {
         int rr = plan.g2r[r];
         if (rr < 0) continue;
@@ -363,10 +389,25 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
             int lr = local(f, rr), lc = local(f, rc);
             if (lr < 0 || lc < 0) throw EngineError(IEMIC_ERR_STATE);
             const FrontDev& fr = plan.fronts[f];
-            plan.asm_src.push_back(q);
-            plan.asm_row.push_back(r);
-            plan.asm_dst.push_back(fr.off + int64_t(lc) * fr.F + lr);
+            ent_q.push_back(q);
+            ent_r.push_back(r);
+            ent_dst.push_back(fr.off + int64_t(lc) * fr.F + lr);
+            ent_front.push_back(fr.lvl);
+            per_level[fr.lvl] += 1;
         }
+    }
+    plan.asm_level_start.assign(H + 1, 0);
+    for (int h = 0; h < H; ++h) plan.asm_level_start[h + 1] = plan.asm_level_start[h] + per_level[h];
+    const size_t na = ent_q.size();
+    plan.asm_src.resize(na);
+    plan.asm_row.resize(na);
+    plan.asm_dst.resize(na);
+    std::vector<int64_t> fill(plan.asm_level_start.begin(), plan.asm_level_start.end() - 1);
+    for (size_t e = 0; e < na; ++e) {
+        const int64_t d = fill[ent_front[e]]++;
+        plan.asm_src[d] = ent_q[e];
+        plan.asm_row[d] = ent_r[e];
+        plan.asm_dst[d] = ent_dst[e];
     }
 }
 
@@ -425,19 +466,53 @@ __global__ void k_assemble(int64_t n, const int* __restrict__ src, const int64_t
     }
 }
 
-// front[parent] += S[child] for the children in `list` (one slot at a time)
+// front[parent] += S[child] for the children in `list` (one slot at a time);
+// the children's contribution blocks come from the ring
 template <class T>
 __global__ void k_extend_add(const FrontDev* __restrict__ fronts, const int* __restrict__ list,
-                             const int* __restrict__ emap, T* __restrict__ front) {
+                             const int* __restrict__ emap, const T* __restrict__ contrib, T* __restrict__ front) {
     const FrontDev c = fronts[list[blockIdx.y]];
     const FrontDev p = fronts[c.parent];
     const int64_t tot = int64_t(c.nb) * c.nb;
     const int* em = emap + c.emap_off;
-    const T* S = front + c.off;
+    const T* S = contrib + c.soff;
     T* P = front + p.off;
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
         int a = int(e % c.nb), b = int(e / c.nb);   // row a, column b of S
-        P[int64_t(em[b]) * p.F + em[a]] += S[int64_t(c.nf + b) * c.F + c.nf + a];
+        P[int64_t(em[b]) * p.F + em[a]] += S[e];
+    }
+}
+
+// End of a level: each front's factors move from the working area to the
+// factor store (its first nf columns as they are, ld F; then rows [0, nf) of
+// columns [nf, F), ld nf) and its contribution block (rows and columns
+// [nf, F)) to the ring (ld nb). Blocks stride over the columns, threads over
+// the rows, four rows in flight per thread.
+template <class T>
+__global__ void __launch_bounds__(256) k_spill(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
+                                               const T* __restrict__ front, T* __restrict__ factor,
+                                               T* __restrict__ contrib) {
+    const FrontDev fr = fronts[lf[blockIdx.y]];
+    const int F = fr.F, nf = fr.nf, nb = fr.nb;
+    for (int c = blockIdx.x; c < F; c += gridDim.x) {
+        const T* src = front + fr.off + int64_t(c) * F;
+        // rows [0, nf) go to lo + r; rows [nf, F) to hi + (r - nf)
+        T* lo = c < nf ? factor + fr.foff + int64_t(c) * F : factor + fr.foff + int64_t(F) * nf + int64_t(c - nf) * nf;
+        T* hi = c < nf ? lo + nf : contrib + fr.soff + int64_t(c - nf) * nb;
+        for (int r0 = threadIdx.x; r0 < F; r0 += 4 * blockDim.x) {
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = r0 + u * blockDim.x;
+                v[u] = r < F ? src[r] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = r0 + u * blockDim.x;
+                if (r < nf) lo[r] = v[u];
+                else if (r < F) hi[r - nf] = v[u];
+            }
+        }
     }
 }
 
@@ -1218,7 +1293,10 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
     }
     __syncthreads();
     const bool live = r < br1;
-    const T* A = front + fr.off + r;
+    // factor store: columns [0, nf) with ld F; the U12/H block (columns
+    // [nf, F), rows [0, nf)) follows them with ld nf
+    const int64_t ld = ST == ST_U12 ? nf : F;
+    const T* A = ST == ST_U12 ? front + fr.foff + int64_t(F - nf) * nf + r : front + fr.foff + r;
     const int g0 = it.col0 + cg * CGW;
     int c0 = g0, c1 = min(bc1, g0 + CGW);
     if (ST == ST_LINV) c1 = min(c1, r);
@@ -1234,7 +1312,7 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
         for (; c + 16 <= c1; c += 16) {
             float a[16];
 #pragma unroll
-            for (int u = 0; u < 16; ++u) a[u] = float(A[int64_t(c + u) * F]);
+            for (int u = 0; u < 16; ++u) a[u] = float(A[int64_t(c + u) * ld]);
 #pragma unroll
             for (int u = 0; u < 16; ++u) {
                 const float2 xv = xs2[c + u - it.col0];
@@ -1243,13 +1321,13 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
         }
         for (; c < c1; ++c) {
             const float2 xv = xs2[c - it.col0];
-            dd_acc(sh, sl, sg * float(A[int64_t(c) * F]), xv.x, xv.y);
+            dd_acc(sh, sl, sg * float(A[int64_t(c) * ld]), xv.x, xv.y);
         }
         out = double(sh) + double(sl);
     } else {
         double acc = 0.0;
 #pragma unroll 4
-        for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * F]) * xs[c - it.col0];
+        for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * ld]) * xs[c - it.col0];
         out = double(sg) * acc;
     }
     if (cg > 0) gsum[cg - 1][rl] = out;
@@ -1386,7 +1464,8 @@ __device__ __forceinline__ void tgemv_stage(const WorkItem& it, const FrontDev& 
     for (int cc = warp; cc < TCOLS; cc += blockDim.x / 32) {
         const int c = it.col0 + cc;
         if (c >= bc1) break;
-        const T* col = front + fr.off + int64_t(c) * F;
+        const T* col = ST == TS_U12 ? front + fr.foff + int64_t(F) * nf + int64_t(c - nf) * nf
+                                    : front + fr.foff + int64_t(c) * F;
         // rows of this column that the stage uses
         int rb = it.row0, re = rend;
         if (ST == TS_UINV) re = min(re, c + 1);          // upper incl. diagonal: r <= c
@@ -1637,7 +1716,9 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_asm_row = upload(lu, plan.asm_row, s);
     lu.d_child_of = upload(lu, child_of, s);
     lu.d_piv = static_cast<int*>(dmalloc(lu, sizeof(int) * size_t(std::max(plan.nred, 1))));
-    lu.d_front = dmalloc(lu, ts * size_t(plan.front_entries));
+    lu.d_front = dmalloc(lu, ts * size_t(plan.work_entries));
+    lu.d_factor = dmalloc(lu, ts * size_t(std::max<int64_t>(plan.factor_entries, 1)));
+    lu.d_contrib = dmalloc(lu, ts * size_t(std::max<int64_t>(plan.contrib_ring * plan.contrib_slot_entries, 1)));
     lu.d_dinv = dmalloc(lu, ts * size_t(plan.dinv_entries));
     lu.d_w = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
     lu.d_red = dmalloc(lu, sizeof(double) * size_t(std::max(plan.nred, 1)));
@@ -1922,18 +2003,25 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
     T* dinv = static_cast<T*>(lu.d_dinv);
     T* scratch = static_cast<T*>(lu.d_scratch);
     const T tau = sizeof(T) == 4 ? T(1e-7) : T(1e-15);
+    T* factor = static_cast<T*>(lu.d_factor);
+    T* contrib = static_cast<T*>(lu.d_contrib);
     cudaEvent_t ev_fs = lu.timer ? lu.timer->start(s) : nullptr;
     equilibrate(lu, rp, ci, values, s);
-    ck(cudaMemsetAsync(front, 0, sizeof(T) * size_t(P.front_entries), s));
     ck(cudaMemsetAsync(lu.d_npert, 0, sizeof(int), s));
-    const int64_t na = int64_t(P.asm_src.size());
-    k_assemble<T><<<blocks_for(na), NT, 0, s>>>(na, lu.d_asm_src, lu.d_asm_dst, lu.d_asm_row, ci, values, lu.d_dr,
-                                                lu.d_dc, front); IEMIC_COUNT_LAUNCH();
     if (ev_fs) lu.timer->stop(ev_fs, s, IEMIC_KC_FACTOR_SETUP, 0.0, 0.0);
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         cudaEvent_t ev_ea = lu.timer ? lu.timer->start(s) : nullptr;
+        // the level's fronts in the working area: J's entries, then the children's contributions
+        ck(cudaMemsetAsync(front, 0, sizeof(T) * size_t(P.level_work[h]), s));
+        {
+            const int64_t a0 = P.asm_level_start[h], na = P.asm_level_start[h + 1] - a0;
+            if (na > 0) {
+                k_assemble<T><<<blocks_for(na), NT, 0, s>>>(na, lu.d_asm_src + a0, lu.d_asm_dst + a0, lu.d_asm_row + a0,
+                                                            ci, values, lu.d_dr, lu.d_dc, front); IEMIC_COUNT_LAUNCH();
+            }
+        }
         for (int sl = 0; sl < 2; ++sl) {
             int nc = lu.child_start[sl][h + 1] - lu.child_start[sl][h];
             if (nc == 0) continue;
@@ -1941,7 +2029,7 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
             for (int c : P.level_children[sl][h]) mx = std::max<int64_t>(mx, int64_t(P.fronts[c].nb) * P.fronts[c].nb);
             dim3 g(blocks_for(mx), nc);
             k_extend_add<T><<<g, NT, 0, s>>>(lu.d_fronts, lu.d_level_children[sl] + lu.child_start[sl][h], lu.d_emap,
-                                             front); IEMIC_COUNT_LAUNCH();
+                                             contrib, front); IEMIC_COUNT_LAUNCH();
         }
         if (ev_ea) lu.timer->stop(ev_ea, s, IEMIC_KC_FACTOR_SETUP, 0.0, 0.0);
         const int maxnf = P.level_maxnf[h], maxF = P.level_maxF[h];
@@ -2056,6 +2144,10 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
             }
         }
         if (ev_inv) lu.timer->stop(ev_inv, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
+        cudaEvent_t ev_sp = lu.timer ? lu.timer->start(s) : nullptr;
+        const int gx = std::max(1, std::min(maxF, (152 * 16 + nfr - 1) / nfr));
+        k_spill<T><<<dim3(gx, nfr), 256, 0, s>>>(lu.d_fronts, lf, front, factor, contrib); IEMIC_COUNT_LAUNCH();
+        if (ev_sp) lu.timer->stop(ev_sp, s, IEMIC_KC_FACTOR_SETUP, 2.0 * sizeof(T) * double(P.level_work[h]), 0.0);
     }
 }
 
@@ -2180,7 +2272,7 @@ static void sweeps_t(NdLu& lu, cudaStream_t s) {
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
     double* WP = static_cast<double*>(lu.d_wp);
-    const T* front = static_cast<const T*>(lu.d_front);
+    const T* front = static_cast<const T*>(lu.d_factor);
     KTimer* kt = lu.timer;
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
@@ -2280,7 +2372,7 @@ static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
     double* WP = static_cast<double*>(lu.d_wp);
-    const T* front = static_cast<const T*>(lu.d_front);
+    const T* front = static_cast<const T*>(lu.d_factor);
     const TStageBufs sb = tstage_bufs(lu);
     k_treduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_dc, r, red); IEMIC_COUNT_LAUNCH();
     for (int h = 0; h < P.nlevels; ++h) {

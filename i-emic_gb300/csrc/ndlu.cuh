@@ -15,8 +15,10 @@ struct FrontDev {
     int nf, nb, F;          // F = nf + nb, leading dimension of the dense front
     int parent;             // -1 at the root
     int red0;               // reduced index of the first own unknown
-    int pad_;
-    int64_t off;            // offset of the column-major F x F front
+    int lvl;                // level (height in the elimination tree)
+    int64_t off;            // offset of the column-major F x F front in the working area of its level
+    int64_t foff;           // offset in the factor store: F x nf (ld F), then the nf x nb block (ld nf)
+    int64_t soff;           // offset of its nb x nb contribution block (ld nb) in the contribution ring
     int64_t voff;           // offset into `vars` (F reduced indices)
     int64_t dinv_off;       // offset of the per-panel inverse diagonal blocks
     int64_t emap_off;       // offset into `emap` (nb parent-local indices)
@@ -41,6 +43,14 @@ struct NdPlan {
     std::vector<int> asm_row;       // its row
     std::vector<int64_t> asm_dst;   // offset in the front storage
     int64_t front_entries = 0, dinv_entries = 0, emap_entries = 0, w_entries = 0;
+    // storage: one working area sized for the largest level (its F x F
+    // fronts), the factor store, and a ring of `contrib_ring` slots of
+    // contribution blocks (a level's blocks live in slot level % ring until
+    // every parent has added them)
+    int64_t work_entries = 0, contrib_slot_entries = 0;
+    int contrib_ring = 1;
+    std::vector<int64_t> level_work;      // per level: its working entries
+    std::vector<int64_t> asm_level_start; // per level: range of its assembly entries
     double flops = 0.0;             // factorisation flop count
     int64_t factor_entries = 0;     // entries the solve phase reads
 };
@@ -68,7 +78,9 @@ struct NdLu {
     double *d_dr = nullptr, *d_dc = nullptr, *d_cmax = nullptr;   // equilibration scalings
     int64_t* d_asm_dst = nullptr;
     int* d_piv = nullptr;                   // per reduced unknown: block-local pivot source
-    void* d_front = nullptr;                // front storage (T)
+    void* d_front = nullptr;                // working area: the F x F fronts of one level (T)
+    void* d_factor = nullptr;               // factor store read by the solves (T)
+    void* d_contrib = nullptr;              // contribution-block ring (T)
     void* d_dinv = nullptr;                 // inverse diagonal panel blocks (T)
     void* d_w = nullptr;                    // solve vectors (T)
     void* d_red = nullptr;                  // reduced rhs / solution (T)

@@ -119,6 +119,25 @@ int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out) {
     out->factor_entries = P.factor_entries;
     out->front_entries = P.front_entries;
     out->factor_flops = P.flops;
+    out->work_entries = P.work_entries;
+    out->contrib_entries = int64_t(P.contrib_ring) * P.contrib_slot_entries;
+    GUARD_END
+}
+
+int iemic_get_fronts(iemic_ocean* h, int cap, int* nf, int* nb, int* level, int* parent, int* count) {
+    if (!h || !count || cap < 0 || (cap > 0 && (!nf || !nb || !level || !parent))) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    h->e.ensure_solver();
+    const NdPlan& P = *h->e.ndplan;
+    for (int lv = 0; lv < P.nlevels; ++lv)
+        for (int f : P.level_fronts[lv]) {
+            if (f >= cap) continue;
+            nf[f] = P.fronts[f].nf;
+            nb[f] = P.fronts[f].nb;
+            level[f] = lv;
+            parent[f] = P.fronts[f].parent;
+        }
+    *count = P.nfronts;
     GUARD_END
 }
 

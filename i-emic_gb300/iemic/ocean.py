@@ -119,7 +119,8 @@ FORCING_FIELDS = ("taux", "tauy", "tatm", "emip", "spert")
 class SolverInfo(ctypes.Structure):
     _fields_ = [("unknowns", ctypes.c_int64), ("reduced_unknowns", ctypes.c_int64), ("fronts", ctypes.c_int64),
                 ("levels", ctypes.c_int64), ("factor_entries", ctypes.c_int64), ("front_entries", ctypes.c_int64),
-                ("factor_flops", ctypes.c_double)]
+                ("factor_flops", ctypes.c_double), ("work_entries", ctypes.c_int64),
+                ("contrib_entries", ctypes.c_int64)]
 
 
 KERNEL_CLASSES = {"factor_gemm": 0, "solve_gemv": 1, "assembly": 2, "spmv": 3, "factor_panel": 4,
@@ -177,6 +178,7 @@ SIGNATURES = {
                                    ctypes.POINTER(ContinuationStats)],
     "iemic_launch_count": [],
     "iemic_kernel_timing_failures": [_VP],
+    "iemic_get_fronts": [_VP, ctypes.c_int, _IP, _IP, _IP, _IP, _IP],
     "iemic_kernel_trace": [_VP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float), _DP, _IP],
 }
 _VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts",
@@ -454,6 +456,16 @@ class Ocean:
             st = KernelStats()
             self._check(self.L.iemic_kernel_stats_get(self._h, k, ctypes.byref(st)), "kernelStats")
             out[name] = _asdict(st)
+        return out
+
+    def fronts(self):
+        """Elimination tree of the factorisation: arrays nf, nb, level, parent per front."""
+        cnt = ctypes.c_int(0)
+        self._check(self.L.iemic_get_fronts(self._h, 0, None, None, None, None, ctypes.byref(cnt)), "fronts")
+        out = {k: np.zeros(cnt.value, np.int32) for k in ("nf", "nb", "level", "parent")}
+        self._check(self.L.iemic_get_fronts(self._h, cnt.value, *(out[k].ctypes.data_as(_IP)
+                                                                  for k in ("nf", "nb", "level", "parent")),
+                                            ctypes.byref(cnt)), "fronts")
         return out
 
     def kernelTrace(self):

@@ -160,3 +160,12 @@ def global_180x76x16():
     """2-degree ocean: 180x76x16, lat +-76, depth 5000 m (stretched)."""
     return dict(BASE, n=180, m=76, l=16, xmin_deg=0.0, xmax_deg=360.0, ymin_deg=-76.0,
                 ymax_deg=76.0, periodic=1, hdim=5000.0, qz=2.25, iza=2, ite=1, its=1)
+
+
+def global_360x160x20():
+    """Global 1-degree ocean: 360x160x20, lon 0-360 periodic, lat +-80,
+    depth 5000 m, stretched levels qz = 2.25; used with a seeded mask whose
+    smooth bathymetry spans 500-5000 m (``seeded_global_mask(cfg, seed,
+    min_depth_frac=0.1)``)."""
+    return dict(BASE, n=360, m=160, l=20, xmin_deg=0.0, xmax_deg=360.0, ymin_deg=-80.0,
+                ymax_deg=80.0, periodic=1, hdim=5000.0, qz=2.25, iza=2, ite=1, its=1)

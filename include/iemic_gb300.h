@@ -145,13 +145,22 @@ int iemic_apply_precon(iemic_ocean* h, int precision, const double* v, double* o
 int iemic_solver_gauge(iemic_ocean* h, int* idx, int capacity, int* count);
 /* Size of the preconditioner's nested-dissection factorisation (no
  * reference counterpart). factor_entries: entries the triangular solves read
- * (per precision multiply by 4 or 8 bytes); front_entries: dense front
- * storage; factor_flops: flops of one factorisation. */
+ * (the factor store; per precision multiply by 4 or 8 bytes); front_entries:
+ * the dense F x F fronts of all levels together; work_entries: the working
+ * area (fronts of the largest level); contrib_entries: the ring of
+ * contribution blocks; factor_flops: flops of one LU (without the explicit
+ * inverses). Device storage of one precision is about (factor_entries +
+ * work_entries + contrib_entries) entries. */
 typedef struct {
     int64_t unknowns, reduced_unknowns, fronts, levels, factor_entries, front_entries;
     double factor_flops;
+    int64_t work_entries, contrib_entries;
 } iemic_solver_info;
 int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out);
+/* The elimination tree of the nested-dissection factorisation: per front its
+ * own unknowns nf, boundary unknowns nb, level (0 = leaves) and parent (-1 at
+ * the root). Copies up to `cap` fronts; *count receives the number of fronts. */
+int iemic_get_fronts(iemic_ocean* h, int cap, int* nf, int* nb, int* level, int* parent, int* count);
 /* Ocean::solve(rhs): x = J^{-1} b (host vectors). */
 int iemic_solve(iemic_ocean* h, const double* b, double* x, const iemic_solve_opts* o,
                 iemic_solve_stats* st);
