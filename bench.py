@@ -47,9 +47,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     ap.add_argument("--cpu-iters", type=int, default=1, help="Newton iterations of the CPU sample")
-    ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1"],
+    ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1", "newton_large"],
                     help="newton1: one Newton iteration per precision from the seeded state, per-kernel-class "
-                         "device times (a short case for profiling)")
+                         "device times (a short case for profiling); newton_large: Newton iterations on the "
+                         "360x160x20 ocean with per-kernel HBM rates")
+    ap.add_argument("--large-steps", type=int, default=5, help="timed Newton iterations of newton_large")
     return ap.parse_args()
 
 
@@ -430,8 +432,82 @@ def run_newton1(args):
     print(json.dumps(out), flush=True)
 
 
+def run_newton_large(args):
+    """Newton iterations on the 1-degree 360x160x20 ocean (6.9 M unknowns):
+    iteration 0 with every kernel timed (per-class device time and HBM rate),
+    then `--large-steps` untimed iterations (F, J, mixed solve to 1e-8,
+    update) through the public host-buffer API. The FP64 path is sized and
+    reported: its factor store alone exceeds the device memory."""
+    import torch
+    from iemic import Ocean
+    from iemic import workloads as W
+    torch.cuda.init()
+    cfg = W.global_360x160x20()
+    lm = W.seeded_global_mask(cfg, 0, min_depth_frac=0.1)
+    oc = Ocean(cfg, lm, forcing=None, starting_parameters=W.STARTING_PARAMETERS)
+    oc.setPar("Combined Forcing", args.setup_comb)
+    x = W.rest_state_with_ts_noise(cfg, 0)
+    info = oc.solverInfo()
+    free, total = torch.cuda.mem_get_info()
+    out = {"mode": "newton_large", "workload": "global_360x160x20", "unknowns": oc.ndim, "solver": info,
+           "device_memory_gb": total / 1e9}
+    peaks = load_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    simt = 2 * 128 * 152 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    steps = []
+    f0 = None
+    for it in range(args.large_steps + 1):
+        timed = it == 0
+        oc.kernelTiming(timed)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        F = oc.computeRHS(x)
+        oc.computeJacobian(x)
+        dx, st = oc.solve(-F, precision=1)
+        x += dx
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        fn = float(np.linalg.norm(F))
+        f0 = fn if f0 is None else f0
+        steps.append({"iter": it, "timed_kernels": timed, "wall_s": wall, "norm_F": fn, "gmres_iters": st["iters"],
+                      "relres": st["relres"], "factor_ms": st["time_factor_ms"], "solve_ms": st["time_solve_ms"],
+                      "status": st["status"]})
+        if timed:
+            ks = oc.kernelStats()
+            kern = {}
+            for k, v in ks.items():
+                if not v["launches"]:
+                    continue
+                e = {"ms": round(v["ms"], 3), "launches": v["launches"]}
+                if v["bytes"] > 0 and v["ms"] > 0 and k != "factor_gemm":
+                    e["gb_s"] = v["bytes"] / (v["ms"] * 1e-3) / 1e9
+                    e["hbm_frac"] = e["gb_s"] / hbm
+                if k == "factor_gemm" and v["ms"] > 0:
+                    e["tflop_s"] = v["flops"] / (v["ms"] * 1e-3) / 1e12
+                    e["simt_frac"] = e["tflop_s"] / simt
+                kern[k] = e
+            out["kernels_iter0"] = kern
+            out["timing_failures"] = oc.kernelTimingFailures()
+        oc.kernelTiming(False)
+        print(json.dumps(steps[-1]), flush=True)
+    run = steps[1:]
+    out["mixed"] = {"steps": steps, "timed_iterations": len(run),
+                    "newton_steps_per_s": len(run) / sum(r["wall_s"] for r in run) if run else None,
+                    "norm_F_first_last": [steps[0]["norm_F"], steps[-1]["norm_F"]]}
+    need64 = 8.0 * (info["factor_entries"] + info["work_entries"] + info["contrib_entries"])
+    out["fp64"] = {"unavailable": "FP64 factor store + working area + contribution ring need %.0f GB of the "
+                                  "device's %.0f GB" % (need64 / 1e9, total / 1e9),
+                   "factor_flops": info["factor_flops"]}
+    free_end, _ = torch.cuda.mem_get_info()
+    out["device_used_gb"] = (total - free_end) / 1e9
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "newton_large":
+        run_newton_large(args)
+        return
     if args.mode == "newton1":
         run_newton1(args)
         return

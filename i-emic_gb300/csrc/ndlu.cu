@@ -141,7 +141,9 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
         if (dry[r]) plan.dry_rows.push_back(r);
     // deferred unknowns: the surface pressure of every (unpinned) water column
     // is eliminated in the root front, so no subdomain block contains a
-    // floating barotropic pressure mode.
+    // floating barotropic pressure mode. (Deferring only a coarse lattice of
+    // them leaves subdomain blocks that block-local pivoting cannot factor:
+    // their pivots break down even in FP64.)
     std::vector<char> deferred(ndim, 0);
     std::vector<int> deferred_list;
     for (int j = 0; j < m; ++j)
@@ -541,8 +543,14 @@ __global__ void __launch_bounds__(32) k_panel_diag(const FrontDev* __restrict__ 
 #pragma unroll
     for (int j = 0; j < B; ++j) {
         if (j < bb) {
-            // pivot: largest |row[j]| over lanes j..bb-1, smallest lane on ties
+            // pivot: largest |row[j]| over lanes j..bb-1, smallest lane on ties;
+            // a NaN ranks below every number (and is counted), so that every
+            // lane agrees on the pivot and it stays inside the block
             T bv = (lane >= j && lane < bb) ? abs(row[j]) : T(-1);
+            if (bv != bv) {
+                bv = T(-0.5);
+                atomicAdd(npert + 1, 1);
+            }
             int br = lane;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -622,7 +630,7 @@ __global__ void k_rowperm_u12(const FrontDev* __restrict__ fronts, const int* __
     __shared__ int perm[B];
     const T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
     for (int e = threadIdx.x; e < B * B; e += blockDim.x) Li[e / B][e % B] = Di[e];
-    if (threadIdx.x < bb) perm[threadIdx.x] = piv[fr.red0 + p + threadIdx.x];
+    if (threadIdx.x < bb) perm[threadIdx.x] = min(max(piv[fr.red0 + p + threadIdx.x], 0), bb - 1);
     __syncthreads();
     int c = blockIdx.x * blockDim.x + threadIdx.x;   // skip the diagonal block
     if (c >= p) c += bb;
@@ -1209,6 +1217,12 @@ __host__ __device__ inline void stage_block(int st, int nf, int F, int& r0, int&
     c1 = st == ST_U12 ? F : nf;
 }
 
+// front-local row that row q of the own block takes after the block-local
+// pivoting (clamped into its block)
+__device__ __forceinline__ int piv_row(const int* __restrict__ piv, const FrontDev& fr, int q, int B) {
+    const int p = (q / B) * B;
+    return p + min(max(piv[fr.red0 + q], 0), min(B, fr.nf - p) - 1);
+}
 // forward prologue: w = [red_C ; 0] + children's update vectors, then the
 // block-local row permutations applied to the own part (into wp). A thread
 // per row: the inverse extend-add map gives each row its children's update
@@ -1240,7 +1254,7 @@ __global__ void __launch_bounds__(NT) k_fwd_gather(const FrontDev* __restrict__ 
     }
     const double wq = fwd_row(fr, q, red, einv, u[0], u[1]);
     W[fr.woff + q] = wq;
-    WP[fr.woff + q] = q < fr.nf ? fwd_row(fr, (q / B) * B + piv[fr.red0 + q], red, einv, u[0], u[1]) : wq;
+    WP[fr.woff + q] = q < fr.nf ? fwd_row(fr, piv_row(piv, fr, q, B), red, einv, u[0], u[1]) : wq;
 }
 // Compensated (double-float) accumulation of a * (xh + xl) into (s, c) with
 // FP32 instructions only: the product's rounding error comes from an FMA and
@@ -1583,8 +1597,7 @@ __global__ void k_tbwd_reduce(const FrontDev* __restrict__ fronts, const int* __
     } else {
         double y = tstage_sum(TS_LINV, f, fr, q, sb);
         if (fused && fr.nb > 0) y += tstage_sum(TS_L21, f, fr, q, sb);
-        const int p = (q / B) * B;
-        yred[fr.red0 + p + piv[fr.red0 + q]] = y;
+        yred[fr.red0 + piv_row(piv, fr, q, B)] = y;
     }
 }
 // reduced transposed right-hand side: column-scaled wet entries
@@ -1725,7 +1738,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     lu.d_dr = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_dc = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_cmax = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
-    lu.d_npert = static_cast<int*>(dmalloc(lu, sizeof(int)));
+    lu.d_npert = static_cast<int*>(dmalloc(lu, 2 * sizeof(int)));
     lu.d_wp = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
     // solve-phase partial-sum buffers (per stage) and work items (per launch
     // group: G/H layout fuses LINV+L21 and UINV+U12; the L21/U12 layout runs
@@ -2007,7 +2020,7 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
     T* contrib = static_cast<T*>(lu.d_contrib);
     cudaEvent_t ev_fs = lu.timer ? lu.timer->start(s) : nullptr;
     equilibrate(lu, rp, ci, values, s);
-    ck(cudaMemsetAsync(lu.d_npert, 0, sizeof(int), s));
+    ck(cudaMemsetAsync(lu.d_npert, 0, 2 * sizeof(int), s));
     if (ev_fs) lu.timer->stop(ev_fs, s, IEMIC_KC_FACTOR_SETUP, 0.0, 0.0);
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
@@ -2213,8 +2226,13 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
         launch_counter() += lu.factor_launches;
     }
     ck(cudaGetLastError());
-    ck(cudaMemcpyAsync(&lu.npert, lu.d_npert, sizeof(int), cudaMemcpyDeviceToHost, s));
-    lu.factored = true;
+    int cnt[2] = {0, 0};
+    ck(cudaMemcpyAsync(cnt, lu.d_npert, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    lu.npert = cnt[0];
+    lu.nnan = cnt[1];
+    lu.factored = lu.nnan == 0;
+    if (!lu.factored) throw EngineError(IEMIC_ERR_NAN);   // the factors overflowed
 }
 
 void ndlu_factor(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {

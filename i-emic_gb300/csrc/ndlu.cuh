@@ -84,7 +84,7 @@ struct NdLu {
     void* d_dinv = nullptr;                 // inverse diagonal panel blocks (T)
     void* d_w = nullptr;                    // solve vectors (T)
     void* d_red = nullptr;                  // reduced rhs / solution (T)
-    int* d_npert = nullptr;                 // perturbed-pivot counter
+    int* d_npert = nullptr;                 // counters: perturbed pivots, NaN pivot candidates
     void* d_wp = nullptr;                   // permuted / gathered solve vectors (FP64)
     // solve phase: partial-sum buffers and per-front offsets per GEMV stage
     // (Linv11, Uinv11, L21 or G, U12 or H), work items per launch group
@@ -117,6 +117,7 @@ struct NdLu {
     const void *fg_rp = nullptr, *fg_ci = nullptr, *fg_val = nullptr;   // arrays the factor graph reads
     long long sweep_launches = 0;           // kernels in the captured sweeps
     int npert = 0;
+    int nnan = 0;
     bool factored = false;
     std::vector<void*> allocs;
     ~NdLu();

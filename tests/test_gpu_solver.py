@@ -112,3 +112,20 @@ def test_kernel_timing_through_graphs(prec):
     fac = [ks[c] for c in ("factor_gemm", "factor_panel", "factor_inverse", "factor_setup")]
     assert sum(k["launches"] for k in fac) > 0 and sum(k["ms"] for k in fac) > 0, ks
     assert ks["solve_gemv"]["launches"] > 0 and ks["solve_gemv"]["ms"] > 0, ks
+
+
+def test_nan_state_is_reported_not_faulted():
+    """A Newton iterate that went to NaN: the factorisation's pivot search stays
+    inside its blocks and the solve reports NaN/Inf instead of touching memory
+    outside the fronts."""
+    from iemic import IemicError
+    g, o, M, x, F, pins = _setup("glob24")
+    xb = x.copy()
+    xb[4::6][::7] = np.nan
+    g.computeJacobian(xb)
+    with pytest.raises(IemicError) as ei:
+        g.solve(-F, precision=1)
+    assert ei.value.code == -4
+    g.computeJacobian(x)                  # the handle recovers with a finite Jacobian
+    sol, st = g.solve(-F, precision=1)
+    assert st["status"] == 0 and st["relres"] <= 1e-8
