@@ -56,6 +56,7 @@ struct Engine {
 
     // solver state (krylov.cu / ndlu.cu)
     NdPlan* ndplan = nullptr;
+    int subst_min_nf = 12288;  // fronts up to this size: whole inverses (ndlu_setup)
     NdLu* lu64 = nullptr;
     NdLu* lu32 = nullptr;
     Krylov* kry = nullptr;

@@ -270,7 +270,7 @@ void Engine::build_preconditioner(int precision) {
     NdLu*& lu = lu_for(precision);
     if (!lu) {
         lu = new NdLu();
-        ndlu_setup(*lu, *ndplan, precision == IEMIC_PREC_MIXED ? 1 : 0);
+        ndlu_setup(*lu, *ndplan, precision == IEMIC_PREC_MIXED ? 1 : 0, subst_min_nf);
         lu->timer = &timer;
     }
     ndlu_factor(*lu, d_rowptr, d_col, d_val, stream);

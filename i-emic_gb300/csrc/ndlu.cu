@@ -944,6 +944,15 @@ __global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* _
 enum { OP_DENSE = 0, OP_LOWER_UNIT = 1, OP_UPPER = 2 };
 constexpr int TRI_SB = 256;   // super-block rows of the row-oriented steps
 constexpr int TRI_KS = 512;   // K piece of a split-K product
+// The solves apply L11 / U11 of a plan whose fronts have at most 12288 own
+// unknowns (the default of iemic_set_substitution_threshold)
+// as whole inverses, one GEMV stage per triangle; a larger plan substitutes
+// over the inverted 256-row diagonal super-blocks. The whole inverses need one GEMV stage per triangle, but their
+// rounding grows with the condition of the whole triangle, which block-local
+// pivoting leaves large: on a 5,005-unknown root front FP32 solves with them
+// reach a relative residual of 0.5 (1e-4 by substitution), and on the
+// 59,470-unknown root of the 360 x 160 x 20 ocean the preconditioner fails.
+
 struct TriTask {
     int64_t a_off, b_off, c_off;   // element offsets: base 0 = front storage, 1 = scratch
     int lda, ldb, ldc, M, N, K;
@@ -1140,23 +1149,6 @@ __global__ void __launch_bounds__(256, 2) k_task_gemm_f32(const TriTask* __restr
     }
 }
 
-// G/H are formed by k_task_gemm_f32 into scratch; the copy puts them in place of L21 / U12
-template <class T, bool HMAT>
-__global__ void k_gh_copy(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ front,
-                          const T* __restrict__ scratch, const int64_t* __restrict__ sc_off) {
-    const FrontDev fr = fronts[lf[blockIdx.y]];
-    const int nf = fr.nf, nb = fr.nb;
-    const int M = HMAT ? nf : nb;
-    const int64_t tot = int64_t(nf) * nb;
-    const T* S = scratch + sc_off[blockIdx.y];
-    T* A = front + fr.off;
-    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
-        int r = int(e % M), c = int(e / M);
-        if (HMAT) A[int64_t(nf + c) * fr.F + r] = S[e];
-        else A[int64_t(c) * fr.F + nf + r] = S[e];
-    }
-}
-
 // ---------------------------------------------------------------------------
 // solve phase
 // ---------------------------------------------------------------------------
@@ -1273,6 +1265,47 @@ __device__ __forceinline__ void dd_acc(float& s, float& c, float a, float xh, fl
     c = __fadd_rn(c, __fadd_rn(err, e));
 }
 
+// sg * sum_{c0 <= c < c1} A[c * ld] x[c - col0] with x staged in shared
+// memory (xs: FP64; xs2: its hi/lo FP32 split for FP32 factors). FP32
+// factors accumulate in compensated double-float, FP64 factors in FP64.
+template <class T>
+__device__ __forceinline__ double row_dot(const T* __restrict__ A, int64_t ld, int c0, int c1, int col0,
+                                          const double* xs, const float2* xs2, float sg) {
+    if (sizeof(T) == 4) {
+        float sh = 0.f, sl = 0.f;
+        // loads are issued 16 columns ahead of the accumulation chain so that
+        // each thread keeps 16 independent HBM reads in flight
+        int c = c0;
+        for (; c + 16 <= c1; c += 16) {
+            float a[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) a[u] = float(A[int64_t(c + u) * ld]);
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const float2 xv = xs2[c + u - col0];
+                dd_acc(sh, sl, sg * a[u], xv.x, xv.y);
+            }
+        }
+        for (; c < c1; ++c) {
+            const float2 xv = xs2[c - col0];
+            dd_acc(sh, sl, sg * float(A[int64_t(c) * ld]), xv.x, xv.y);
+        }
+        return double(sh) + double(sl);
+    }
+    double acc = 0.0;
+#pragma unroll 4
+    for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * ld]) * xs[c - col0];
+    return double(sg) * acc;
+}
+__device__ __forceinline__ void stage_x(double v, double* xs, float2* xs2, int q, bool fp32) {
+    if (fp32) {
+        const float h = __double2float_rn(v);
+        xs2[q] = make_float2(h, __double2float_rn(v - double(h)));
+    } else {
+        xs[q] = v;
+    }
+}
+
 // Partial GEMV products of one stage over a (GT-row, GC-column) tile;
 // ST_LINV uses the strict lower part plus the unit diagonal, ST_UINV the
 // upper part, ST_L21 and ST_U12 the dense blocks with a minus sign. Partial
@@ -1317,33 +1350,7 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
     else if (ST == ST_UINV) c0 = max(c0, r);
     if (!live) c1 = c0;
     const float sg = (ST == ST_L21 || ST == ST_U12) ? -1.f : 1.f;
-    double out;
-    if (sizeof(T) == 4) {
-        float sh = 0.f, sl = 0.f;
-        // loads are issued 16 columns ahead of the accumulation chain so that
-        // each thread keeps 16 independent HBM reads in flight
-        int c = c0;
-        for (; c + 16 <= c1; c += 16) {
-            float a[16];
-#pragma unroll
-            for (int u = 0; u < 16; ++u) a[u] = float(A[int64_t(c + u) * ld]);
-#pragma unroll
-            for (int u = 0; u < 16; ++u) {
-                const float2 xv = xs2[c + u - it.col0];
-                dd_acc(sh, sl, sg * a[u], xv.x, xv.y);
-            }
-        }
-        for (; c < c1; ++c) {
-            const float2 xv = xs2[c - it.col0];
-            dd_acc(sh, sl, sg * float(A[int64_t(c) * ld]), xv.x, xv.y);
-        }
-        out = double(sh) + double(sl);
-    } else {
-        double acc = 0.0;
-#pragma unroll 4
-        for (int c = c0; c < c1; ++c) acc += double(A[int64_t(c) * ld]) * xs[c - it.col0];
-        out = double(sg) * acc;
-    }
+    double out = row_dot<T>(A, ld, c0, c1, it.col0, xs, xs2, sg);
     if (cg > 0) gsum[cg - 1][rl] = out;
     __syncthreads();
     if (cg > 0 || !live) return;
@@ -1352,6 +1359,92 @@ __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& f
         out += sizeof(T) == 4 ? xs2[r - it.col0].x + double(xs2[r - it.col0].y) : xs[r - it.col0];
     part[part_off[it.front] + int64_t(it.chunk) * (br1 - br0) + (r - br0)] = out;
 }
+// Block substitution over the inverted 256-row diagonal super-blocks of a
+// front's L11 / U11 (the forward solves): for super-block s,
+//   lower (forward sweep):  y_s = Linv_ss (w_s - L(s, 0:s) y)
+//   upper (backward sweep): x_s = Uinv_ss (t_s - U(s, s+1:) x)
+// Only the 256 x 256 diagonal blocks are inverted, so rounding errors grow
+// with their condition, not with that of the whole triangle (which
+// block-local pivoting leaves large). One sub-step per super-block: the
+// off-diagonal products of every front of the level as tiled partial GEMVs
+// (k_sub_gemv), then the diagonal blocks (k_sub_diag, one CTA per front).
+constexpr int SB = 256;
+static_assert(SB == GC, "a GEMV column chunk is one super-block");
+struct SubDiag {
+    int front, s, pbase, nch;   // super-block s; its nch partial chunks at part[pbase + c * SB + r]
+};
+// off-diagonal partials of one sub-step: an item is a (GT-row, GC-column)
+// tile, `stage` holds the front's partial base; x (y or x of the
+// super-blocks already done) is read from the front's solve vector W
+template <class T, bool UP>
+__global__ void __launch_bounds__(GR) k_sub_gemv(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
+                                                 const T* __restrict__ factor, const double* __restrict__ W,
+                                                 double* __restrict__ part) {
+    const WorkItem it = items[blockIdx.x];
+    const FrontDev fr = fronts[it.front];
+    const int F = fr.F, nf = fr.nf;
+    const int s = it.row0 / SB, r1 = min(nf, (s + 1) * SB);
+    const int cend = UP ? nf : s * SB;
+    const int rl = threadIdx.x % GT, cg = threadIdx.x / GT;
+    const int r = it.row0 + rl;
+    __shared__ double xs[GC];
+    __shared__ float2 xs2[GC];
+    __shared__ double gsum[NCG - 1][GT];
+    const double* x = W + fr.woff;
+    for (int q = threadIdx.x; q < GC; q += GR) stage_x(it.col0 + q < cend ? x[it.col0 + q] : 0.0, xs, xs2, q, sizeof(T) == 4);
+    __syncthreads();
+    const bool live = r < r1;
+    const int g0 = it.col0 + cg * CGW;
+    const int c0 = g0, c1 = live ? min(cend, g0 + CGW) : g0;
+    double out = row_dot<T>(factor + fr.foff + r, F, c0, c1, it.col0, xs, xs2, -1.f);
+    if (cg > 0) gsum[cg - 1][rl] = out;
+    __syncthreads();
+    if (cg > 0 || !live) return;
+    for (int k = 0; k < NCG - 1; ++k) out += gsum[k][rl];
+    part[it.stage + int64_t(it.chunk) * SB + (r - s * SB)] = out;
+}
+// diagonal super-block: t = rhs + partials, then y = Linv_ss t (unit lower)
+// or x = Uinv_ss t; 1024 threads = 256 rows x 4 column groups of 64
+constexpr int SDT = 1024, SDG = SDT / SB, SDW = SB / SDG;
+template <class T, bool UP>
+__global__ void __launch_bounds__(SDT) k_sub_diag(const FrontDev* __restrict__ fronts, const SubDiag* __restrict__ items,
+                                                  const T* __restrict__ factor, const double* __restrict__ part,
+                                                  double* __restrict__ W, double* __restrict__ WP,
+                                                  double* __restrict__ xred) {
+    const SubDiag it = items[blockIdx.x];
+    const FrontDev fr = fronts[it.front];
+    const int F = fr.F, s0 = it.s * SB, ns = min(SB, fr.nf - s0);
+    const int rl = threadIdx.x % SB, cg = threadIdx.x / SB;
+    __shared__ double ts[SB];
+    __shared__ float2 ts2[SB];
+    __shared__ double gsum[SDG - 1][SB];
+    if (cg == 0) {
+        double t = 0.0;
+        if (rl < ns) {
+            t = WP[fr.woff + s0 + rl];
+            const double* p = part + it.pbase + rl;
+            for (int c = 0; c < it.nch; ++c) t += p[int64_t(c) * SB];
+        }
+        ts[rl] = t;
+        if (sizeof(T) == 4) stage_x(t, ts, ts2, rl, true);
+    }
+    __syncthreads();
+    const bool live = rl < ns;
+    int c0 = cg * SDW, c1 = min(ns, c0 + SDW);
+    if (UP) c0 = max(c0, rl);   // upper part incl. the diagonal
+    else c1 = min(c1, rl);      // strict lower part (unit diagonal added below)
+    if (!live) c1 = c0;
+    double out = row_dot<T>(factor + fr.foff + int64_t(s0) * F + s0 + rl, F, c0, max(c0, c1), 0, ts, ts2, 1.f);
+    if (cg > 0) gsum[cg - 1][rl] = out;
+    __syncthreads();
+    if (cg > 0 || !live) return;
+    for (int k = 0; k < SDG - 1; ++k) out += gsum[k][rl];
+    if (!UP) out += ts[rl];
+    W[fr.woff + s0 + rl] = out;
+    if (UP) xred[fr.red0 + s0 + rl] = out;
+    else WP[fr.woff + s0 + rl] = out;
+}
+
 template <class T>
 __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
                                                   const T* __restrict__ front, const double* __restrict__ X, StageBufs sb) {
@@ -1378,22 +1471,6 @@ __device__ __forceinline__ double stage_sum(int st, int f, const FrontDev& fr, i
     double s = 0.0;
     for (int c = 0; c < nch; ++c) s += p[int64_t(c) * rows];
     return s;
-}
-// fused epilogues of the G/H layout: forward rows [0, F), backward rows [0, nf)
-template <bool BWD>
-__global__ void k_fused_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
-                               double* __restrict__ W, double* __restrict__ WP, double* __restrict__ xred) {
-    const int f = lf[blockIdx.y];
-    const FrontDev fr = fronts[f];
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!BWD) {
-        if (r >= fr.F) return;
-        if (r < fr.nf) W[fr.woff + r] = stage_sum(ST_LINV, f, fr, r, sb);
-        else WP[fr.woff + r] += stage_sum(ST_L21, f, fr, r, sb);
-    } else {
-        if (r >= fr.nf) return;
-        xred[fr.red0 + r] = stage_sum(ST_UINV, f, fr, r, sb) + (fr.nb > 0 ? stage_sum(ST_U12, f, fr, r, sb) : 0.0);
-    }
 }
 template <int ST>
 __global__ void k_stage_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
@@ -1635,11 +1712,13 @@ int blocks_for(int64_t work, int per = NT) {
 // drivers
 // ===========================================================================
 NdLu::~NdLu() {
-    if (sweep_exec) cudaGraphExecDestroy(sweep_exec);
+    for (int k = 0; k < 2; ++k) {
+        if (sweep_exec[k]) cudaGraphExecDestroy(sweep_exec[k]);
+        if (sweep_exec_timed[k]) cudaGraphExecDestroy(sweep_exec_timed[k]);
+    }
     if (factor_exec) cudaGraphExecDestroy(factor_exec);
-    if (sweep_exec_timed) cudaGraphExecDestroy(sweep_exec_timed);
     if (factor_exec_timed) cudaGraphExecDestroy(factor_exec_timed);
-    for (auto* t : {&factor_tmpl, &sweep_tmpl})
+    for (auto* t : {&factor_tmpl, &sweep_tmpl[0], &sweep_tmpl[1]})
         for (const KTimer::Rec& r : *t) {
             cudaEventDestroy(r.a);
             cudaEventDestroy(r.b);
@@ -1663,7 +1742,7 @@ static void* dmalloc(NdLu& lu, size_t bytes) {
     return d;
 }
 
-void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
+void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
     cudaStream_t s = 0;
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_STRIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_BAND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
@@ -1743,7 +1822,6 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
     // solve-phase partial-sum buffers (per stage) and work items (per launch
     // group: G/H layout fuses LINV+L21 and UINV+U12; the L21/U12 layout runs
     // the four stages as separate groups)
-    lu.gh = prec == 1;
     std::vector<WorkItem> items[NSTAGE];
     for (int st = 0; st < NSTAGE; ++st) {
         std::vector<int64_t> off(plan.nfronts, 0);
@@ -1760,7 +1838,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         lu.d_stage_part[st] = static_cast<double*>(dmalloc(lu, pb));
         ck(cudaMemsetAsync(lu.d_stage_part[st], 0, pb, s));
     }
-    const int group_of[NSTAGE] = {0, 3, lu.gh ? 0 : 1, lu.gh ? 3 : 2};   // by stage
+    const int group_of[NSTAGE] = {0, 3, 1, 2};   // by stage
     std::vector<WorkItem> gitems[4];
     for (int g = 0; g < 4; ++g) {
         lu.group_start[g].assign(1, 0);
@@ -1788,6 +1866,50 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         for (int g = 0; g < 4; ++g) lu.group_start[g].push_back(int(gitems[g].size()));
     }
     for (int g = 0; g < 4; ++g) lu.d_group_items[g] = upload(lu, gitems[g], s);
+    // block substitution: per level and sub-step k, the fronts with more than
+    // k super-blocks take super-block s = k (lower) or s = nsb - 1 - k (upper)
+    {
+        int64_t pmax = 0;
+        for (int up = 0; up < 2; ++up) {
+            std::vector<WorkItem> its;
+            std::vector<SubDiag> dgs;
+            lu.sub_item_start[up].assign(plan.nlevels, {});
+            lu.sub_diag_start[up].assign(plan.nlevels, {});
+            lu.sub_bytes[up].assign(plan.nlevels, {});
+            for (int h = 0; h < plan.nlevels; ++h) {
+                const int nk = (plan.level_maxnf[h] + SB - 1) / SB;
+                for (int k = 0; k < nk; ++k) {
+                    lu.sub_item_start[up][h].push_back(int(its.size()));
+                    lu.sub_diag_start[up][h].push_back(int(dgs.size()));
+                    int64_t pb = 0;
+                    double by = 0.0;
+                    for (int f : plan.level_fronts[h]) {
+                        const FrontDev& fr = plan.fronts[f];
+                        const int nsb = (fr.nf + SB - 1) / SB;
+                        if (k >= nsb) continue;
+                        const int sblk = up ? nsb - 1 - k : k;
+                        const int r0 = sblk * SB, r1 = std::min(fr.nf, r0 + SB);
+                        const int cb = up ? r1 : 0, ce = up ? fr.nf : r0;   // off-diagonal columns
+                        const int nch = (ce - cb + SB - 1) / SB;
+                        if (pb + int64_t(SB) * nch > INT32_MAX) throw EngineError(IEMIC_ERR_NOMEM);
+                        for (int ch = 0; ch < nch; ++ch)
+                            for (int r = r0; r < r1; r += GT) its.push_back(WorkItem{f, r, cb + ch * SB, ch, int(pb)});
+                        dgs.push_back(SubDiag{f, sblk, int(pb), nch});
+                        pb += int64_t(SB) * nch;
+                        const double m = r1 - r0;
+                        by += double(ts) * (m * (ce - cb) + m * (m + (up ? 1 : -1)) / 2);
+                    }
+                    pmax = std::max(pmax, pb);
+                    lu.sub_bytes[up][h].push_back(by);
+                }
+                lu.sub_item_start[up][h].push_back(int(its.size()));
+                lu.sub_diag_start[up][h].push_back(int(dgs.size()));
+            }
+            lu.d_sub_items[up] = upload(lu, its, s);
+            lu.d_sub_diag[up] = upload(lu, dgs, s);
+        }
+        lu.d_sub_part = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(pmax, 1))));
+    }
     // transposed solve: partial buffers per stage (columns x row chunks) and
     // work items per launch group: G/H layout fuses UINV^T+H^T (group 0) and
     // LINV^T+G^T (group 3); the L21/U12 layout runs four separate groups
@@ -1807,7 +1929,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         ck(cudaMemsetAsync(lu.d_tstage_part[st], 0, pb, s));
     }
     {
-        const int tgroup_of[4] = {0, lu.gh ? 0 : 1, lu.gh ? 3 : 2, 3};   // TS_UINV, TS_U12, TS_LINV, TS_L21
+        const int tgroup_of[4] = {0, 1, 2, 3};   // TS_UINV, TS_U12, TS_LINV, TS_L21
         std::vector<WorkItem> titems[4];
         for (int g = 0; g < 4; ++g) lu.tgroup_start[g].assign(1, 0);
         for (int h = 0; h < plan.nlevels; ++h) {
@@ -1830,19 +1952,6 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         }
         for (int g = 0; g < 4; ++g) lu.d_tgroup_items[g] = upload(lu, titems[g], s);
     }
-    // factorisation scratch (per level, per front) for G/H
-    std::vector<int64_t> scg;
-    int64_t mx = 0;
-    for (int h = 0; h < plan.nlevels; ++h) {
-        int64_t b = 0;
-        for (int f : plan.level_fronts[h]) {
-            const FrontDev& fr = plan.fronts[f];
-            scg.push_back(b);
-            if (lu.gh) b += int64_t(fr.nf) * fr.nb;
-        }
-        mx = std::max(mx, b);
-    }
-    lu.d_sc_gh = upload(lu, scg, s);
     // recursive triangular inversion: tasks and 64x64 tiles per (level, merge
     // size, phase); phase-1 products go to a scratch area of their own
     {
@@ -1850,11 +1959,11 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
         std::vector<TriTile> tiles;
         std::vector<SplitGroup> groups;
         const int tile = prec ? FG_TM : 64;   // k_task_gemm_f32 / k_tri_gemm tile size
-        int64_t tmax = 0;
+        int64_t tmax = 0, tmax2 = 0;
         lu.tri_ranges.clear();
-        lu.gh_ranges.clear();
+        lu.inv2_ranges.clear();
         for (int h = 0; h < plan.nlevels; ++h) {
-            std::vector<std::pair<int, int>> lv;
+            std::vector<std::pair<int, int>> lv, lv2;
             auto emit = [&](const TriTask& t) {
                 const int id = int(tasks.size());
                 tasks.push_back(t);
@@ -1895,6 +2004,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                 }
             }
             // (2) block-row steps over the super-blocks (row-oriented inversion,
+            //     run on demand in the factor store, for transposed solves,
             //     whose rounding involves one large inverse per product):
             //     lower, top down:  X[Ri, 0:i0] = -Linv_ii (L[Ri, 0:i0] X[0:i0, 0:i0])
             //     upper, bottom up: Y[Ri, i1:nf] = -Uinv_ii (U[Ri, i1:nf] Y[i1:nf, i1:nf])
@@ -1918,7 +2028,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                             toff += int64_t(m) * w * ns;
                             if (phase == 0) {   // T = L[Ri, 0:r0] * X[0:r0, 0:r0]   (m x w), split along K
                                 for (int sp = 0; sp < ns; ++sp) {
-                                    TriTask tk{fr.off + r0, fr.off, tcur + int64_t(sp) * m * w, F, F, m, m, w, w,
+                                    TriTask tk{fr.foff + r0, fr.foff, tcur + int64_t(sp) * m * w, F, F, m, m, w, w,
                                                OP_DENSE, OP_LOWER_UNIT, 0, 0, 1, 1.f};
                                     tk.k0 = sp * TRI_KS;
                                     tk.k1 = ns > 1 ? std::min(w, (sp + 1) * TRI_KS) : w;
@@ -1926,7 +2036,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                                 }
                                 if (ns > 1) groups.push_back(SplitGroup{tcur, int64_t(m) * w, ns});
                             } else {            // X[Ri, 0:r0] = -Linv_ii * T
-                                emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + r0, F, m, F, m, w, m,
+                                emit(TriTask{fr.foff + int64_t(r0) * F + r0, tcur, fr.foff + r0, F, m, F, m, w, m,
                                              OP_LOWER_UNIT, OP_DENSE, 0, 1, 0, -1.f});
                             }
                         }
@@ -1938,7 +2048,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                             toff += int64_t(m) * w * ns;
                             if (phase == 0) {   // T = U[Ri, r1:nf] * Y[r1:nf, r1:nf]   (m x w), split along K
                                 for (int sp = 0; sp < ns; ++sp) {
-                                    TriTask tk{fr.off + int64_t(r1) * F + r0, fr.off + int64_t(r1) * F + r1,
+                                    TriTask tk{fr.foff + int64_t(r1) * F + r0, fr.foff + int64_t(r1) * F + r1,
                                                tcur + int64_t(sp) * m * w, F, F, m, m, w, w, OP_DENSE, OP_UPPER,
                                                0, 0, 1, 1.f};
                                     tk.k0 = sp * TRI_KS;
@@ -1947,49 +2057,32 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec) {
                                 }
                                 if (ns > 1) groups.push_back(SplitGroup{tcur, int64_t(m) * w, ns});
                             } else {            // Y[Ri, r1:nf] = -Uinv_ii * T
-                                emit(TriTask{fr.off + int64_t(r0) * F + r0, tcur, fr.off + int64_t(r1) * F + r0,
+                                emit(TriTask{fr.foff + int64_t(r0) * F + r0, tcur, fr.foff + int64_t(r1) * F + r0,
                                              F, m, F, m, w, m, OP_UPPER, OP_DENSE, 0, 1, 0, -1.f});
                             }
                         }
                     }
-                    tmax = std::max(tmax, toff);
-                    lv.push_back({tb, int(tiles.size())});
-                    if (int(groups.size()) > gb) lv.push_back({-1 - gb, -1 - int(groups.size())});   // split-K reduce
+                    tmax2 = std::max(tmax2, toff);
+                    lv2.push_back({tb, int(tiles.size())});
+                    if (int(groups.size()) > gb) lv2.push_back({-1 - gb, -1 - int(groups.size())});   // split-K reduce
                 }
             }
             lu.tri_ranges.push_back(lv);
-            // G = L21 * Linv11 and H = Uinv11 * U12 (FP32 factors) into the G/H scratch
-            std::vector<std::pair<int, int>> gv;
-            if (lu.gh) {
-                for (int which = 0; which < 2; ++which) {
-                    const int tb = int(tiles.size());
-                    int64_t goff = 0;
-                    for (int f : plan.level_fronts[h]) {
-                        const FrontDev& fr = plan.fronts[f];
-                        const int nf = fr.nf, nb = fr.nb, F = fr.F;
-                        const int64_t cur = goff;
-                        goff += int64_t(nf) * nb;
-                        if (nf == 0 || nb == 0) continue;
-                        if (which == 0)   // G (nb x nf)
-                            emit(TriTask{fr.off + nf, fr.off, cur, F, F, nb, nb, nf, nf, OP_DENSE, OP_LOWER_UNIT,
-                                         0, 0, 1, 1.f});
-                        else              // H (nf x nb)
-                            emit(TriTask{fr.off, fr.off + int64_t(nf) * F, cur, F, F, nf, nf, nb, nf, OP_UPPER,
-                                         OP_DENSE, 0, 0, 1, 1.f});
-                    }
-                    gv.push_back({tb, int(tiles.size())});
-                }
-            }
-            lu.gh_ranges.push_back(gv);
+            lu.inv2_ranges.push_back(lv2);
         }
         lu.d_tri_tasks = upload(lu, tasks, s);
         lu.d_tri_tiles = upload(lu, tiles, s);
         lu.d_tri_groups = upload(lu, groups, s);
         lu.d_tri_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax, 1)));
+        lu.inv2_scratch_entries = tmax2;
+        int maxnf = 0;
+        for (int h = 0; h < plan.nlevels; ++h) maxnf = std::max(maxnf, plan.level_maxnf[h]);
+        lu.subst = maxnf > subst_min_nf;
+        if (!lu.subst) lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
         lu.tri_flops = 0.0;
         for (const TriTask& t : tasks) lu.tri_flops += double(t.M) * t.N * t.K;   // ~ half are structural zeros
     }
-    lu.d_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(mx, 1)));
+
     ck(cudaStreamSynchronize(s));
 }
 
@@ -2009,12 +2102,49 @@ static void equilibrate(NdLu& lu, const int* rp, const int* ci, const double* va
     }
 }
 
+// One launch range of the triangular-inversion tasks (k >= 0: task tiles;
+// negative: the split-K reduce of a group range); `base` is the storage the
+// tasks' offsets refer to (working area or factor store).
+template <class T>
+static void tri_range(NdLu& lu, const std::pair<int, int>& rg, T* base, T* scr, cudaStream_t s) {
+    if (rg.first < 0) {   // split-K reduce of groups [-1-first, -1-second)
+        const int g0 = -1 - rg.first, g1 = -1 - rg.second;
+        k_split_reduce<T><<<dim3(64, std::min(g1 - g0, 65535)), 256, 0, s>>>(
+            static_cast<const SplitGroup*>(lu.d_tri_groups) + g0, g1 - g0, scr); IEMIC_COUNT_LAUNCH();
+        return;
+    }
+    if (rg.second <= rg.first) return;
+    const TriTask* tk = static_cast<const TriTask*>(lu.d_tri_tasks);
+    const TriTile* tl = static_cast<const TriTile*>(lu.d_tri_tiles) + rg.first;
+    if constexpr (sizeof(T) == 4)
+        k_task_gemm_f32<<<rg.second - rg.first, 256, FG_SMEM, s>>>(tk, tl, reinterpret_cast<float*>(base),
+                                                                   reinterpret_cast<float*>(scr));
+    else
+        k_tri_gemm<T><<<rg.second - rg.first, 256, 0, s>>>(tk, tl, base, scr);
+    IEMIC_COUNT_LAUNCH();
+}
+
+// Whole-block inverses Linv11 / Uinv11 in the factor store (the row-oriented
+// steps over the super-blocks), for the transposed sweeps; run once per
+// factorisation, when the first transposed solve needs them.
+template <class T>
+static void to_full_inverse(NdLu& lu, cudaStream_t s) {
+    if (lu.full_inverse) return;
+    if (!lu.d_inv2_scratch)
+        lu.d_inv2_scratch = dmalloc(lu, sizeof(T) * size_t(std::max<int64_t>(lu.inv2_scratch_entries, 1)));
+    cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
+    for (const auto& lv : lu.inv2_ranges)
+        for (const auto& rg : lv) tri_range<T>(lu, rg, static_cast<T*>(lu.d_factor), static_cast<T*>(lu.d_inv2_scratch), s);
+    if (ev) lu.timer->stop(ev, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
+    ck(cudaGetLastError());
+    lu.full_inverse = true;
+}
+
 template <class T, int B>
 static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {
     const NdPlan& P = *lu.plan;
     T* front = static_cast<T*>(lu.d_front);
     T* dinv = static_cast<T*>(lu.d_dinv);
-    T* scratch = static_cast<T*>(lu.d_scratch);
     const T tau = sizeof(T) == 4 ? T(1e-7) : T(1e-15);
     T* factor = static_cast<T*>(lu.d_factor);
     T* contrib = static_cast<T*>(lu.d_contrib);
@@ -2123,44 +2253,19 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
         const int maxblk = (maxnf + B - 1) / B;
         cudaEvent_t ev_inv = lu.timer ? lu.timer->start(s) : nullptr;
         k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
-        auto task_launch = [&](const std::pair<int, int>& rg, T* scr) {
-            if (rg.first < 0) {   // split-K reduce of groups [-1-first, -1-second)
-                const int g0 = -1 - rg.first, g1 = -1 - rg.second;
-                k_split_reduce<T><<<dim3(64, std::min(g1 - g0, 65535)), 256, 0, s>>>(
-                    static_cast<const SplitGroup*>(lu.d_tri_groups) + g0, g1 - g0, scr); IEMIC_COUNT_LAUNCH();
-                return;
-            }
-            if (rg.second <= rg.first) return;
-            const TriTask* tk = static_cast<const TriTask*>(lu.d_tri_tasks);
-            const TriTile* tl = static_cast<const TriTile*>(lu.d_tri_tiles) + rg.first;
-            if constexpr (sizeof(T) == 4)
-                k_task_gemm_f32<<<rg.second - rg.first, 256, FG_SMEM, s>>>(tk, tl, reinterpret_cast<float*>(front),
-                                                                           reinterpret_cast<float*>(scr));
-            else
-                k_tri_gemm<T><<<rg.second - rg.first, 256, 0, s>>>(tk, tl, front, scr);
-            IEMIC_COUNT_LAUNCH();
-        };
-        for (const auto& rg : lu.tri_ranges[h]) task_launch(rg, static_cast<T*>(lu.d_tri_scratch));
-        if (lu.gh) {
-            const int64_t* scg = lu.d_sc_gh + lu.level_start[h];
-            int64_t mt = 0, mnb = 0;
-            for (int f : P.level_fronts[h]) {
-                const FrontDev& fr = P.fronts[f];
-                mt = std::max<int64_t>(mt, int64_t((fr.nf + 63) / 64) * ((fr.nb + 63) / 64));
-                mnb = std::max<int64_t>(mnb, int64_t(fr.nf) * fr.nb);
-            }
-            if (mt > 0) {
-                task_launch(lu.gh_ranges[h][0], scratch);
-                k_gh_copy<T, false><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-                task_launch(lu.gh_ranges[h][1], scratch);
-                k_gh_copy<T, true><<<dim3(blocks_for(mnb), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, scratch, scg); IEMIC_COUNT_LAUNCH();
-            }
-        }
+        // merges inside the 256-row super-blocks: each diagonal super-block
+        // of L11 / U11 then holds its inverse, the solves substitute over them
+        for (const auto& rg : lu.tri_ranges[h]) tri_range<T>(lu, rg, front, static_cast<T*>(lu.d_tri_scratch), s);
         if (ev_inv) lu.timer->stop(ev_inv, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
         cudaEvent_t ev_sp = lu.timer ? lu.timer->start(s) : nullptr;
         const int gx = std::max(1, std::min(maxF, (152 * 16 + nfr - 1) / nfr));
         k_spill<T><<<dim3(gx, nfr), 256, 0, s>>>(lu.d_fronts, lf, front, factor, contrib); IEMIC_COUNT_LAUNCH();
         if (ev_sp) lu.timer->stop(ev_sp, s, IEMIC_KC_FACTOR_SETUP, 2.0 * sizeof(T) * double(P.level_work[h]), 0.0);
+        if (!lu.subst) {   // whole inverses of L11 / U11 in the factor store
+            cudaEvent_t ev2 = lu.timer ? lu.timer->start(s) : nullptr;
+            for (const auto& rg : lu.inv2_ranges[h]) tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_inv2_scratch), s);
+            if (ev2) lu.timer->stop(ev2, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
+        }
     }
 }
 
@@ -2231,6 +2336,7 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
     ck(cudaStreamSynchronize(s));
     lu.npert = cnt[0];
     lu.nnan = cnt[1];
+    lu.full_inverse = !lu.subst;
     lu.factored = lu.nnan == 0;
     if (!lu.factored) throw EngineError(IEMIC_ERR_NAN);   // the factors overflowed
 }
@@ -2269,23 +2375,34 @@ static void launch_reduce(NdLu& lu, int h, double* W, double* WP, double* red, c
     k_stage_reduce<ST><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red); IEMIC_COUNT_LAUNCH();
     if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
 }
-template <bool BWD>
-static void launch_fused_reduce(NdLu& lu, int h, double* W, double* WP, double* red, cudaStream_t s) {
-    const NdPlan& P = *lu.plan;
-    const int nfr = lu.level_start[h + 1] - lu.level_start[h];
-    const int* lf = lu.d_level_fronts + lu.level_start[h];
-    const int rows = BWD ? P.level_maxnf[h] : P.level_maxF[h];
-    if (rows <= 0) return;
+// the sub-steps of the block substitution of level h (UP: backward sweep)
+template <class T, bool UP>
+static void sub_steps(NdLu& lu, int h, const T* factor, double* W, double* WP, double* red, cudaStream_t s) {
+    const auto& is = lu.sub_item_start[UP][h];
+    const auto& ds = lu.sub_diag_start[UP][h];
     KTimer* kt = lu.timer;
-    cudaEvent_t ev = kt ? kt->start(s) : nullptr;
-    k_fused_reduce<BWD><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red); IEMIC_COUNT_LAUNCH();
-    if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+    for (size_t k = 0; k + 1 < is.size(); ++k) {
+        cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+        const int ni = is[k + 1] - is[k], nd = ds[k + 1] - ds[k];
+        if (ni > 0) {
+            k_sub_gemv<T, UP><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_sub_items[UP]) + is[k],
+                                                factor, W, lu.d_sub_part); IEMIC_COUNT_LAUNCH();
+        }
+        if (nd > 0) {
+            k_sub_diag<T, UP><<<nd, SDT, 0, s>>>(lu.d_fronts, static_cast<const SubDiag*>(lu.d_sub_diag[UP]) + ds[k],
+                                                 factor, lu.d_sub_part, W, WP, red); IEMIC_COUNT_LAUNCH();
+        }
+        const double by = lu.sub_bytes[UP][h][k];
+        if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_GEMV, by, 2.0 * by / sizeof(T));
+    }
 }
 
 // The forward and backward sweeps over the levels: internal buffers only
-// (red -> red), so they can be captured once into a CUDA graph.
+// (red -> red), so they can be captured once into a CUDA graph. The
+// triangles L11 / U11 are applied by block substitution (full = false) or,
+// once their whole inverses exist (after a transposed solve), as GEMVs.
 template <class T, int B>
-static void sweeps_t(NdLu& lu, cudaStream_t s) {
+static void sweeps_t(NdLu& lu, bool full, cudaStream_t s) {
     const NdPlan& P = *lu.plan;
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
@@ -2301,15 +2418,14 @@ static void sweeps_t(NdLu& lu, cudaStream_t s) {
                                                                                 lu.d_einv, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        if (lu.gh) {
-            launch_group<T>(lu, 0, h, front, WP, s);
-            launch_fused_reduce<false>(lu, h, W, WP, red, s);
-        } else {
+        if (full) {
             launch_group<T>(lu, 0, h, front, WP, s);
             launch_reduce<ST_LINV>(lu, h, W, WP, red, s);
-            launch_group<T>(lu, 1, h, front, WP, s);
-            launch_reduce<ST_L21>(lu, h, W, WP, red, s);
+        } else {
+            sub_steps<T, false>(lu, h, front, W, WP, red, s);
         }
+        launch_group<T>(lu, 1, h, front, WP, s);
+        launch_reduce<ST_L21>(lu, h, W, WP, red, s);
     }
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
@@ -2319,14 +2435,13 @@ static void sweeps_t(NdLu& lu, cudaStream_t s) {
             k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        if (lu.gh) {
-            launch_group<T>(lu, 3, h, front, WP, s);
-            launch_fused_reduce<true>(lu, h, W, WP, red, s);
-        } else {
-            launch_group<T>(lu, 2, h, front, WP, s);
-            launch_reduce<ST_U12>(lu, h, W, WP, red, s);
+        launch_group<T>(lu, 2, h, front, WP, s);
+        launch_reduce<ST_U12>(lu, h, W, WP, red, s);
+        if (full) {
             launch_group<T>(lu, 3, h, front, WP, s);
             launch_reduce<ST_UINV>(lu, h, W, WP, red, s);
+        } else {
+            sub_steps<T, true>(lu, h, front, W, WP, red, s);
         }
     }
 }
@@ -2342,24 +2457,25 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
                                                             lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
+    const int fm = lu.full_inverse ? 1 : 0;
     if (kt && kt->on) {
-        timed_graph(lu, lu.sweep_exec_timed, lu.sweep_tmpl, lu.sweep_launches_timed, s,
-                    [&] { sweeps_t<T, B>(lu, s); });
+        timed_graph(lu, lu.sweep_exec_timed[fm], lu.sweep_tmpl[fm], lu.sweep_launches_timed[fm], s,
+                    [&] { sweeps_t<T, B>(lu, fm == 1, s); });
     } else {
-        if (!lu.sweep_exec) {
+        if (!lu.sweep_exec[fm]) {
             cudaGraph_t g = nullptr;
             ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             const long long n0 = launch_counter();
-            sweeps_t<T, B>(lu, s);
-            lu.sweep_launches = launch_counter() - n0;
+            sweeps_t<T, B>(lu, fm == 1, s);
+            lu.sweep_launches[fm] = launch_counter() - n0;
             launch_counter() = n0;
             ck(cudaStreamEndCapture(s, &g));
-            const cudaError_t e = cudaGraphInstantiate(&lu.sweep_exec, g, 0);
+            const cudaError_t e = cudaGraphInstantiate(&lu.sweep_exec[fm], g, 0);
             cudaGraphDestroy(g);
             ck(e);
         }
-        ck(cudaGraphLaunch(lu.sweep_exec, s));
-        launch_counter() += lu.sweep_launches;
+        ck(cudaGraphLaunch(lu.sweep_exec[fm], s));
+        launch_counter() += lu.sweep_launches[fm];
     }
     {
         cudaEvent_t ev = kt ? kt->start(s) : nullptr;
@@ -2390,6 +2506,7 @@ static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
     double* WP = static_cast<double*>(lu.d_wp);
+    to_full_inverse<T>(lu, s);
     const T* front = static_cast<const T*>(lu.d_factor);
     const TStageBufs sb = tstage_bufs(lu);
     k_treduce_rhs<TV><<<blocks_for(P.nred), NT, 0, s>>>(P.nred, lu.d_r2g, lu.d_dc, r, red); IEMIC_COUNT_LAUNCH();
@@ -2398,29 +2515,20 @@ static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr);
         k_tfwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, red, W, WP); IEMIC_COUNT_LAUNCH();
-        if (lu.gh) {
-            launch_tgroup<T>(lu, 0, h, front, WP, s);   // UINV^T and H^T on c
-            k_tfwd_reduce<2><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
-        } else {
-            launch_tgroup<T>(lu, 0, h, front, WP, s);   // v = UINV^T c
-            k_tfwd_reduce<0><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
-            launch_tgroup<T>(lu, 1, h, front, WP, s);   // -U12^T v
-            k_tfwd_reduce<1><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
-        }
+        launch_tgroup<T>(lu, 0, h, front, WP, s);   // v = UINV^T c
+        k_tfwd_reduce<0><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
+        launch_tgroup<T>(lu, 1, h, front, WP, s);   // -U12^T v
+        k_tfwd_reduce<1><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
     }
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr), gN((P.level_maxnf[h] + NT - 1) / NT, nfr);
         k_tbwd_gather<<<gF, NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
-        if (lu.gh) {
-            launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T v and -G^T y_B
-        } else {
-            launch_tgroup<T>(lu, 2, h, front, WP, s);   // -L21^T y_B
-            k_tbwd_reduce<0><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
-            launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T t
-        }
-        k_tbwd_reduce<1><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, lu.gh ? 1 : 0, B); IEMIC_COUNT_LAUNCH();
+        launch_tgroup<T>(lu, 2, h, front, WP, s);   // -L21^T y_B
+        k_tbwd_reduce<0><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
+        launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T t
+        k_tbwd_reduce<1><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
     }
     k_texpand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dr, red, r, z); IEMIC_COUNT_LAUNCH();
     ck(cudaGetLastError());

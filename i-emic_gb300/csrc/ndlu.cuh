@@ -87,14 +87,21 @@ struct NdLu {
     int* d_npert = nullptr;                 // counters: perturbed pivots, NaN pivot candidates
     void* d_wp = nullptr;                   // permuted / gathered solve vectors (FP64)
     // solve phase: partial-sum buffers and per-front offsets per GEMV stage
-    // (Linv11, Uinv11, L21 or G, U12 or H), work items per launch group
-    bool gh = false;                        // fronts hold G/H (FP32) instead of L21/U12 (FP64)
+    // (Linv11, Uinv11, L21, U12), work items per launch group
     double* d_stage_part[4] = {nullptr, nullptr, nullptr, nullptr};
     int64_t* d_stage_off[4] = {nullptr, nullptr, nullptr, nullptr};
     void* d_group_items[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<int> group_start[4];        // per level offsets into d_group_items
     std::vector<double> group_bytes[4];     // per level: factor bytes the group reads
-    int64_t* d_sc_gh = nullptr;             // G/H scratch offsets per front (by level)
+    // block substitution over the inverted 256-row diagonal super-blocks
+    // (forward solves), [0] lower (forward sweep), [1] upper (backward sweep):
+    // per level and sub-step the off-diagonal GEMV tiles and the per-front
+    // diagonal items; one partial-sum buffer reused by every sub-step
+    void* d_sub_items[2] = {nullptr, nullptr};
+    void* d_sub_diag[2] = {nullptr, nullptr};
+    std::vector<std::vector<int>> sub_item_start[2], sub_diag_start[2];   // [level][sub-step], one past the end
+    std::vector<std::vector<double>> sub_bytes[2];                        // factor bytes per sub-step
+    double* d_sub_part = nullptr;
     // transposed solve: partial buffers per transposed stage, items per group
     double* d_tstage_part[4] = {nullptr, nullptr, nullptr, nullptr};
     int64_t* d_tstage_off[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -103,19 +110,23 @@ struct NdLu {
     // recursive triangular inversion: tasks, tiles, per level the tile ranges
     // of its launches, and the scratch of the first product of each merge
     void *d_tri_tasks = nullptr, *d_tri_tiles = nullptr, *d_tri_scratch = nullptr, *d_tri_groups = nullptr;
-    std::vector<std::vector<std::pair<int, int>>> tri_ranges;
-    std::vector<std::vector<std::pair<int, int>>> gh_ranges;   // per level: G tiles, H tiles (FP32 factors)
+    std::vector<std::vector<std::pair<int, int>>> tri_ranges;    // merges (factorisation)
+    std::vector<std::vector<std::pair<int, int>>> inv2_ranges;   // whole-block inverses (on demand)
+    int64_t inv2_scratch_entries = 0;
+    void* d_inv2_scratch = nullptr;
+    bool subst = false;                     // solves substitute over super-blocks (large fronts)
+    bool full_inverse = false;              // L11 / U11 replaced by their whole inverses
     double tri_flops = 0.0;
-    void* d_scratch = nullptr;
-    cudaGraphExec_t sweep_exec = nullptr; // captured forward + backward level sweeps
     cudaGraphExec_t factor_exec = nullptr;  // captured factorisation
+    // captured forward + backward level sweeps, [0] block substitution, [1] whole inverses
+    cudaGraphExec_t sweep_exec[2] = {nullptr, nullptr};
     // the same graphs with timing event nodes (kernel timing on)
-    cudaGraphExec_t factor_exec_timed = nullptr, sweep_exec_timed = nullptr;
-    std::vector<KTimer::Rec> factor_tmpl, sweep_tmpl;
-    long long factor_launches_timed = 0, sweep_launches_timed = 0;
+    cudaGraphExec_t factor_exec_timed = nullptr, sweep_exec_timed[2] = {nullptr, nullptr};
+    std::vector<KTimer::Rec> factor_tmpl, sweep_tmpl[2];
+    long long factor_launches_timed = 0, sweep_launches_timed[2] = {0, 0};
     long long factor_launches = 0;
     const void *fg_rp = nullptr, *fg_ci = nullptr, *fg_val = nullptr;   // arrays the factor graph reads
-    long long sweep_launches = 0;           // kernels in the captured sweeps
+    long long sweep_launches[2] = {0, 0};   // kernels in the captured sweeps
     int npert = 0;
     int nnan = 0;
     bool factored = false;
@@ -123,7 +134,9 @@ struct NdLu {
     ~NdLu();
 };
 
-void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec);
+// subst_min_nf: fronts up to this many own unknowns keep whole inverses of
+// L11 / U11; a plan with a larger front substitutes over 256-row super-blocks
+void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf);
 // values: FP64 CSR values of J (equilibrated in FP64, then cast to the factor precision)
 void ndlu_factor(NdLu& lu, const int* row_ptr, const int* col_idx, const double* values, cudaStream_t s);
 // z = M^{-1} r on global-indexed vectors (float if vec_fp32, else double);

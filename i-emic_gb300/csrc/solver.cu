@@ -124,6 +124,20 @@ int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out) {
     GUARD_END
 }
 
+int iemic_set_substitution_threshold(iemic_ocean* h, int max_inverse_nf) {
+    if (!h || max_inverse_nf < 0) return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    if (max_inverse_nf != h->e.subst_min_nf) {
+        ck(cudaStreamSynchronize(h->e.stream));
+        delete h->e.lu64;
+        delete h->e.lu32;
+        h->e.lu64 = h->e.lu32 = nullptr;
+        h->e.subst_min_nf = max_inverse_nf;
+        h->e.fact64_stale = h->e.fact32_stale = true;
+    }
+    GUARD_END
+}
+
 int iemic_get_fronts(iemic_ocean* h, int cap, int* nf, int* nb, int* level, int* parent, int* count) {
     if (!h || !count || cap < 0 || (cap > 0 && (!nf || !nb || !level || !parent))) return IEMIC_ERR_ARG;
     GUARD_BEGIN

@@ -178,6 +178,7 @@ SIGNATURES = {
                                    ctypes.POINTER(ContinuationStats)],
     "iemic_launch_count": [],
     "iemic_kernel_timing_failures": [_VP],
+    "iemic_set_substitution_threshold": [_VP, ctypes.c_int],
     "iemic_get_fronts": [_VP, ctypes.c_int, _IP, _IP, _IP, _IP, _IP],
     "iemic_kernel_trace": [_VP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float), _DP, _IP],
 }
@@ -457,6 +458,10 @@ class Ocean:
             self._check(self.L.iemic_kernel_stats_get(self._h, k, ctypes.byref(st)), "kernelStats")
             out[name] = _asdict(st)
         return out
+
+    def setSubstitutionThreshold(self, max_inverse_nf):
+        """Fronts up to this many own unknowns use whole inverses; larger plans substitute over 256-row blocks."""
+        self._check(self.L.iemic_set_substitution_threshold(self._h, int(max_inverse_nf)), "setSubstitutionThreshold")
 
     def fronts(self):
         """Elimination tree of the factorisation: arrays nf, nb, level, parent per front."""

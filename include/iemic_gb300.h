@@ -157,6 +157,13 @@ typedef struct {
     int64_t work_entries, contrib_entries;
 } iemic_solver_info;
 int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out);
+/* Triangular solves of the preconditioner: a factorisation whose fronts have
+ * at most `max_inverse_nf` own unknowns (default 12288) stores the whole
+ * inverses of their diagonal triangles and applies them as GEMVs; a larger one
+ * substitutes over inverted 256-row diagonal blocks (more sequential steps,
+ * rounding bounded by the blocks' condition instead of the whole triangle's).
+ * A change discards the current factorisations. */
+int iemic_set_substitution_threshold(iemic_ocean* h, int max_inverse_nf);
 /* The elimination tree of the nested-dissection factorisation: per front its
  * own unknowns nf, boundary unknowns nb, level (0 = leaves) and parent (-1 at
  * the root). Copies up to `cap` fronts; *count receives the number of fronts. */

@@ -129,3 +129,24 @@ def test_nan_state_is_reported_not_faulted():
     g.computeJacobian(x)                  # the handle recovers with a finite Jacobian
     sol, st = g.solve(-F, precision=1)
     assert st["status"] == 0 and st["relres"] <= 1e-8
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_block_substitution_solves(prec):
+    """Substitution over inverted 256-row diagonal blocks (forced on a small
+    case): forward solves match the oracle; a transposed solve then builds the
+    whole inverses in place, and forward solves keep matching afterwards."""
+    g, o, M, x, F, pins = _setup("glob24")
+    g.setSubstitutionThreshold(0)
+    sol, st = g.solve(-F, precision=prec)
+    assert st["status"] == 0 and st["relres"] <= 1e-8 and st["factorizations"] == 1, st
+    ref = M.solve(-F)
+    assert np.linalg.norm(sol - ref) / np.linalg.norm(ref) <= 1e-5
+    assert np.all(sol[pins] == 0.0)
+    b = M.J.T @ np.random.default_rng(3).normal(size=g.ndim)
+    lam, st = g.solve(b, precision=prec, transpose=1)
+    assert st["status"] == 0 and np.linalg.norm(M.J.T @ lam - b) <= 1e-8 * np.linalg.norm(b), st
+    sol2, st = g.solve(-F, precision=prec, reuse_preconditioner=1)
+    assert st["factorizations"] == 0 and st["relres"] <= 1e-8, st
+    assert np.linalg.norm(sol2 - ref) / np.linalg.norm(ref) <= 1e-5
+    g.setSubstitutionThreshold(12288)
