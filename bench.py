@@ -52,6 +52,8 @@ def parse():
                          "device times (a short case for profiling); newton_large: Newton iterations on the "
                          "360x160x20 ocean with per-kernel HBM rates")
     ap.add_argument("--large-steps", type=int, default=5, help="timed Newton iterations of newton_large")
+    ap.add_argument("--subst-threshold", type=int, default=None,
+                    help="newton_large: largest front kept as whole inverses (default: the library's)")
     return ap.parse_args()
 
 
@@ -445,11 +447,14 @@ def run_newton_large(args):
     cfg = W.global_360x160x20()
     lm = W.seeded_global_mask(cfg, 0, min_depth_frac=0.1)
     oc = Ocean(cfg, lm, forcing=None, starting_parameters=W.STARTING_PARAMETERS)
+    if args.subst_threshold is not None:
+        oc.setSubstitutionThreshold(args.subst_threshold)
     oc.setPar("Combined Forcing", args.setup_comb)
     x = W.rest_state_with_ts_noise(cfg, 0)
     info = oc.solverInfo()
     free, total = torch.cuda.mem_get_info()
     out = {"mode": "newton_large", "workload": "global_360x160x20", "unknowns": oc.ndim, "solver": info,
+           "subst_threshold": args.subst_threshold,
            "device_memory_gb": total / 1e9}
     peaks = load_peaks()
     hbm = peaks.get("hbm_gbs", 6800.0)
