@@ -526,71 +526,99 @@ template <class T, int B>
 __global__ void __launch_bounds__(32) k_panel_diag(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
                                                    int p, T* __restrict__ front, T* __restrict__ dinv,
                                                    int* __restrict__ piv, T tau, int* __restrict__ npert) {
-    // One warp per front; lane r holds row r of the bb x bb diagonal block in
-    // registers (all loops fully unrolled, so the row stays in registers).
-    // Pivot search, row maxima and the broadcast of the pivot row are warp
-    // shuffles; there is no shared-memory round trip in the elimination.
+    // One warp per front; lane r keeps row r of the block in registers for
+    // the whole elimination (rows are not exchanged: `pos` records the step at
+    // which a row became the pivot, and the rows are written out in that
+    // order). Each step finds the pivot by warp shuffles, the pivot lane
+    // publishes its row in shared memory, and every lane reads it back with
+    // vector loads. The step loop is not unrolled, to keep the kernel small.
     static_assert(B == 32, "one lane per row");
     const FrontDev fr = fronts[lf[blockIdx.x]];
     if (fr.nf <= p) return;
     const int bb = min(B, fr.nf - p), F = fr.F, lane = threadIdx.x;
     const unsigned full = 0xffffffffu;
+    __shared__ __align__(16) T prow[B];        // the current pivot row
+    __shared__ T S[B][B + 1];                   // the factored block in pivot order (padded rows)
     T* A = front + fr.off + int64_t(p) * F + p;
     T row[B];
 #pragma unroll
     for (int c = 0; c < B; ++c) row[c] = (lane < bb && c < bb) ? A[int64_t(c) * F + lane] : (lane == c ? T(1) : T(0));
-    int perm = lane;
+    int pos = lane < bb ? -1 : lane;            // padding rows keep their place
+#pragma unroll 1
+    for (int j = 0; j < bb; ++j) {
+        T a = T(0);
 #pragma unroll
-    for (int j = 0; j < B; ++j) {
-        if (j < bb) {
-            // pivot: largest |row[j]| over lanes j..bb-1, smallest lane on ties;
-            // a NaN ranks below every number (and is counted), so that every
-            // lane agrees on the pivot and it stays inside the block
-            T bv = (lane >= j && lane < bb) ? abs(row[j]) : T(-1);
-            if (bv != bv) {
-                bv = T(-0.5);
-                atomicAdd(npert + 1, 1);
-            }
-            int br = lane;
+        for (int c = 0; c < B; ++c)
+            if (c == j) a = row[c];
+        // pivot: largest |a| over the rows not yet used, smallest lane on ties;
+        // a NaN ranks below every number (and is counted), so that every lane
+        // agrees on the pivot and it stays inside the block
+        T bv = pos < 0 ? abs(a) : T(-1);
+        if (bv != bv) {
+            bv = T(-0.5);
+            atomicAdd(npert + 1, 1);
+        }
+        int br = lane;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const T ov = __shfl_xor_sync(full, bv, o);
-                const int orr = __shfl_xor_sync(full, br, o);
-                if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
-            }
-            const int pr = br;
-            if (pr != j) {   // swap rows j and pr (uniform branch)
-                const int src = lane == j ? pr : (lane == pr ? j : lane);
-#pragma unroll
-                for (int c = 0; c < B; ++c) row[c] = __shfl_sync(full, row[c], src);
-                perm = __shfl_sync(full, perm, src);
-            }
-            // pivot row maximum from column j on
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_xor_sync(full, bv, o);
+            const int orr = __shfl_xor_sync(full, br, o);
+            if (ov > bv || (ov == bv && orr < br)) { bv = ov; br = orr; }
+        }
+        const int pr = br;
+        if (lane == pr) {
+            pos = j;
+            // pivot row maximum from column j on, perturbation of a tiny pivot
             T sc = T(0);
 #pragma unroll
-            for (int c = j; c < B; ++c) sc = max(sc, abs(row[c]));
-            sc = __shfl_sync(full, (lane < bb) ? sc : T(0), j);
-            T d = __shfl_sync(full, row[j], j);
+            for (int c = 0; c < B; ++c)
+                if (c >= j) sc = max(sc, abs(row[c]));
+            T d = a;
             if (!(abs(d) > tau * sc)) {
                 d = (d < T(0) ? -tau : tau) * (sc > T(0) ? sc : T(1));
-                if (lane == j) {
-                    row[j] = d;
-                    atomicAdd(npert, 1);
+                atomicAdd(npert, 1);
+#pragma unroll
+                for (int c = 0; c < B; ++c)
+                    if (c == j) row[c] = d;
+            }
+#pragma unroll
+            for (int c = 0; c < B; ++c) prow[c] = row[c];
+        }
+        __syncwarp();
+        if (pos < 0) {   // eliminate below the pivot: l = a / d, row -= l * prow (columns > j)
+            T u[B];
+#pragma unroll
+            for (int c = 0; c < B; c += 16 / sizeof(T)) {
+                if (sizeof(T) == 4) {
+                    const float4 v = *reinterpret_cast<const float4*>(&prow[c]);
+                    u[c] = T(v.x); u[c + 1] = T(v.y); u[c + 2] = T(v.z); u[c + 3] = T(v.w);
+                } else {
+                    const double2 v = *reinterpret_cast<const double2*>(&prow[c]);
+                    u[c] = T(v.x); u[c + 1] = T(v.y);
                 }
             }
-            if (lane > j && lane < bb) row[j] /= d;
+            T d = T(0);
 #pragma unroll
-            for (int c = j + 1; c < B; ++c) {
-                const T u = __shfl_sync(full, row[c], j);
-                if (lane > j && lane < bb && c < bb) row[c] -= row[j] * u;
+            for (int c = 0; c < B; ++c)
+                if (c == j) d = u[c];
+            const T l = a / d;
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
+                if (c > j) row[c] -= l * u[c];
+                else if (c == j) row[c] = l;
             }
         }
+        __syncwarp();
     }
+    // rows in pivot order: S[pos] = row; the factors go back to the front
+#pragma unroll
+    for (int c = 0; c < B; ++c) S[pos][c] = row[c];
+    __syncwarp();
     if (lane < bb) {
 #pragma unroll
         for (int c = 0; c < B; ++c)
-            if (c < bb) A[int64_t(c) * F + lane] = row[c];
-        piv[fr.red0 + p + lane] = perm;
+            if (c < bb) A[int64_t(c) * F + pos] = row[c];
+        piv[fr.red0 + p + pos] = lane;
     }
     // inverses: lane c computes column c of Linv (unit lower) and of Uinv
     T* Di = dinv + fr.dinv_off + int64_t(p / B) * 2 * B * B;
@@ -599,18 +627,17 @@ __global__ void __launch_bounds__(32) k_panel_diag(const FrontDev* __restrict__ 
     for (int r = 0; r < B; ++r) {
         T t = (r == lane) ? T(1) : T(0);
 #pragma unroll
-        for (int q = 0; q < r; ++q) t -= __shfl_sync(full, row[q], r) * x[q];   // L[r][q] from lane r
+        for (int q = 0; q < r; ++q) t -= S[r][q] * x[q];
         x[r] = (r > lane) ? t : (r == lane ? T(1) : T(0));
     }
 #pragma unroll
     for (int r = 0; r < B; ++r) Di[r * B + lane] = (r < bb && lane < bb) ? x[r] : T(0);
 #pragma unroll
     for (int r = B - 1; r >= 0; --r) {
-        const T urr = __shfl_sync(full, row[r], r);
         T t = (r == lane) ? T(1) : T(0);
 #pragma unroll
-        for (int q = r + 1; q < B; ++q) t -= __shfl_sync(full, row[q], r) * x[q];   // U[r][q] from lane r
-        x[r] = (r <= lane && r < bb && lane < bb) ? t / urr : T(0);
+        for (int q = r + 1; q < B; ++q) t -= S[r][q] * x[q];
+        x[r] = (r <= lane && r < bb && lane < bb) ? t / S[r][r] : T(0);
     }
 #pragma unroll
     for (int r = 0; r < B; ++r) Di[B * B + r * B + lane] = (r < bb && lane < bb) ? x[r] : T(0);
@@ -2194,11 +2221,15 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
                 by += double(sizeof(T)) * (2.0 * Mr * Nc + Mr * K + K * Nc);
             }
         };
+        constexpr int TS = 64;   // tile of the strip and band updates
+        auto tiles_s = [](int n) { return (std::max(n, 1) + TS - 1) / TS; };
         auto fgemm = [&](int mode, dim3 grid, int p, int P0) {
             if constexpr (sizeof(T) == 4) {
                 float* fp = reinterpret_cast<float*>(front);
-                if (mode == GM_STRIP) k_fgemm_f32<GM_STRIP><<<grid, 256, FG_SMEM, s>>>(lu.d_fronts, lf, p, P0, fp);
-                else if (mode == GM_BAND) k_fgemm_f32<GM_BAND><<<grid, 256, FG_SMEM, s>>>(lu.d_fronts, lf, p, P0, fp);
+                // the K = 32 strip and band updates are skinny (one side <= OB):
+                // 64 x 64 tiles give them four times the CTAs of 128 x 128
+                if (mode == GM_STRIP) k_fgemm<float, GM_STRIP, TS><<<grid, 256, 0, s>>>(lu.d_fronts, lf, p, P0, fp);
+                else if (mode == GM_BAND) k_fgemm<float, GM_BAND, TS><<<grid, 256, 0, s>>>(lu.d_fronts, lf, p, P0, fp);
                 else k_fgemm_f32<GM_TRAIL><<<grid, 256, FG_SMEM, s>>>(lu.d_fronts, lf, p, P0, fp);
             } else {
                 if (mode == GM_STRIP) k_fgemm<T, GM_STRIP, TM><<<grid, 256, 0, s>>>(lu.d_fronts, lf, p, P0, front);
@@ -2229,7 +2260,7 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
                 if (ev_pn) lu.timer->stop(ev_pn, s, IEMIC_KC_FACTOR_PANEL, 0.0, 0.0);
                 if (p + B < pend) {   // update inside the outer panel
                     timed_gemm(GM_STRIP, p, P0, [&] {
-                        fgemm(GM_STRIP, dim3(tiles(maxF - p) * tiles(OB), nfr), p, P0);
+                        fgemm(GM_STRIP, dim3(tiles_s(maxF - p) * tiles_s(OB), nfr), p, P0);
                     });
                 }
             }
@@ -2241,7 +2272,7 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
                 if (ev_pn) lu.timer->stop(ev_pn, s, IEMIC_KC_FACTOR_PANEL, 0.0, 0.0);
                 if (p + B < pend) {
                     timed_gemm(GM_BAND, p, P0, [&] {
-                        fgemm(GM_BAND, dim3(tiles(OB) * tiles(maxF - P0), nfr), p, P0);
+                        fgemm(GM_BAND, dim3(tiles_s(OB) * tiles_s(maxF - P0), nfr), p, P0);
                     });
                 }
             }
