@@ -1639,24 +1639,26 @@ __device__ __forceinline__ double tstage_sum(int st, int f, const FrontDev& fr, 
 }
 // leaves -> root prologue: W = [c_own ; 0] + children's update vectors (no permutation)
 __global__ void __launch_bounds__(NT) k_tfwd_gather(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
-                                                    const int* __restrict__ child_of, const int* __restrict__ emap,
+                                                    const int* __restrict__ child_of, const int2* __restrict__ einv,
                                                     const double* __restrict__ red, double* __restrict__ W,
                                                     double* __restrict__ WP) {
-    const int f = lf[blockIdx.x];
+    // a thread per front row: own rhs (or 0), then the children's update
+    // vectors (kept in W) added in slot order through the inverse map
+    const int f = lf[blockIdx.y];
     const FrontDev fr = fronts[f];
-    const int F = fr.F, nf = fr.nf, tid = threadIdx.x;
-    double* w = WP + fr.woff;
-    for (int q = tid; q < F; q += NT) w[q] = q < nf ? red[fr.red0 + q] : 0.0;
-    __syncthreads();
-    for (int s = 0; s < 2; ++s) {
-        const int c = child_of[2 * f + s];
-        if (c < 0) continue;
-        const FrontDev ch = fronts[c];
-        const double* u = W + ch.woff + ch.nf;   // child's update vector (kept in W)
-        const int* em = emap + ch.emap_off;
-        for (int a = tid; a < ch.nb; a += NT) w[em[a]] += u[a];
-        __syncthreads();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= fr.F) return;
+    double w = q < fr.nf ? red[fr.red0 + q] : 0.0;
+    const int2 a = einv[fr.woff + q];
+    if (a.x >= 0) {
+        const FrontDev ch = fronts[child_of[2 * f]];
+        w += W[ch.woff + ch.nf + a.x];
     }
+    if (a.y >= 0) {
+        const FrontDev ch = fronts[child_of[2 * f + 1]];
+        w += W[ch.woff + ch.nf + a.y];
+    }
+    WP[fr.woff + q] = w;
 }
 // leaves -> root epilogues. Two-stage: (UINV) v -> W[own], WP[own]; (U12)
 // W[B] = c_B + sums. Fused (H): both from the same launch.
@@ -2545,7 +2547,7 @@ static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
         const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr);
-        k_tfwd_gather<<<nfr, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_emap, red, W, WP); IEMIC_COUNT_LAUNCH();
+        k_tfwd_gather<<<gF, NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of, lu.d_einv, red, W, WP); IEMIC_COUNT_LAUNCH();
         launch_tgroup<T>(lu, 0, h, front, WP, s);   // v = UINV^T c
         k_tfwd_reduce<0><<<gF, NT, 0, s>>>(lu.d_fronts, lf, sb, W, WP); IEMIC_COUNT_LAUNCH();
         launch_tgroup<T>(lu, 1, h, front, WP, s);   // -U12^T v

@@ -150,3 +150,21 @@ def test_block_substitution_solves(prec):
     assert st["factorizations"] == 0 and st["relres"] <= 1e-8, st
     assert np.linalg.norm(sol2 - ref) / np.linalg.norm(ref) <= 1e-5
     g.setSubstitutionThreshold(12288)
+
+
+def test_elimination_tree_listing():
+    """iemic_get_fronts agrees with the solver's size report: one root, parents
+    on higher levels, own unknowns summing to the reduced system."""
+    g, o, M, x, F, pins = _setup("glob24")
+    fr = g.fronts()
+    info = g.solverInfo()
+    nf, nb = fr["nf"].astype(np.int64), fr["nb"].astype(np.int64)
+    assert len(nf) == info["fronts"]
+    assert nf.sum() == info["reduced_unknowns"]
+    roots = np.nonzero(fr["parent"] < 0)[0]
+    assert len(roots) == 1 and nb[roots[0]] == 0
+    child = fr["parent"] >= 0
+    assert np.all(fr["level"][fr["parent"][child]] > fr["level"][child])
+    assert fr["level"].max() + 1 == info["levels"]
+    assert (nf * nf + 2 * nf * nb).sum() == info["factor_entries"]
+    assert ((nf + nb) ** 2).sum() == info["front_entries"]
