@@ -473,15 +473,17 @@ __global__ void k_assemble(int64_t n, const int* __restrict__ src, const int64_t
 template <class T>
 __global__ void k_extend_add(const FrontDev* __restrict__ fronts, const int* __restrict__ list,
                              const int* __restrict__ emap, const T* __restrict__ contrib, T* __restrict__ front) {
+    // blocks stride over the columns b of S, threads over its rows a
     const FrontDev c = fronts[list[blockIdx.y]];
     const FrontDev p = fronts[c.parent];
-    const int64_t tot = int64_t(c.nb) * c.nb;
+    const int nb = c.nb;
     const int* em = emap + c.emap_off;
     const T* S = contrib + c.soff;
     T* P = front + p.off;
-    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
-        int a = int(e % c.nb), b = int(e / c.nb);   // row a, column b of S
-        P[int64_t(em[b]) * p.F + em[a]] += S[e];
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        T* pc = P + int64_t(em[b]) * p.F;
+        const T* sc = S + int64_t(b) * nb;
+        for (int a = threadIdx.x; a < nb; a += blockDim.x) pc[em[a]] += sc[a];
     }
 }
 
@@ -2197,9 +2199,9 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
         for (int sl = 0; sl < 2; ++sl) {
             int nc = lu.child_start[sl][h + 1] - lu.child_start[sl][h];
             if (nc == 0) continue;
-            int64_t mx = 0;
-            for (int c : P.level_children[sl][h]) mx = std::max<int64_t>(mx, int64_t(P.fronts[c].nb) * P.fronts[c].nb);
-            dim3 g(blocks_for(mx), nc);
+            int mx = 1;
+            for (int c : P.level_children[sl][h]) mx = std::max(mx, P.fronts[c].nb);
+            dim3 g(std::max(1, std::min(mx, (152 * 16 + nc - 1) / nc)), nc);
             k_extend_add<T><<<g, NT, 0, s>>>(lu.d_fronts, lu.d_level_children[sl] + lu.child_start[sl][h], lu.d_emap,
                                              contrib, front); IEMIC_COUNT_LAUNCH();
         }
