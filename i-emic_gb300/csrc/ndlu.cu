@@ -827,19 +827,21 @@ __global__ void __launch_bounds__(256) k_fgemm(const FrontDev* __restrict__ fron
 // FP32 version of k_fgemm: 128 x 128 tiles, 8 x 8 outputs per thread in two
 // 4 x 4 quadrants (rows tx*4 + {0..3} and 64 + tx*4 + {0..3}, likewise for
 // the columns) so that every operand read from shared memory is a float4.
-// Operands are staged with cp.async (zero-filled outside the block) into two
-// buffers in dynamic shared memory: the copy of the next 32-deep K chunk is
-// in flight while the current one is multiplied. B is stored k-major with
+// Operands are staged with cp.async (zero-filled outside the block) into three
+// buffers in dynamic shared memory: the copies of the next two 32-deep K
+// chunks are in flight while the current one is multiplied. B is stored k-major with
 // its 4-column groups XOR-swizzled by (k & 7) to spread the transposing
 // copies over the banks.
 constexpr int FG_TM = 128;
-constexpr size_t FG_SMEM = sizeof(float) * 2 * 2 * 32 * FG_TM;   // 64 KiB
+constexpr int FG_NBUF = 3;
+constexpr size_t FG_SMEM = sizeof(float) * FG_NBUF * 2 * 32 * FG_TM;   // 96 KiB: two CTAs per SM
 __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
 template <int MODE>
 __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict__ fronts, const int* __restrict__ lf,
                                                       int p, int P0, float* __restrict__ front) {
@@ -868,7 +870,7 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
     float* A = front + fr.off;
     extern __shared__ __align__(16) float fg_smem[];
     auto As = [&](int buf, int k) { return fg_smem + (buf * 32 + k) * TM; };
-    auto Bs = [&](int buf, int k) { return fg_smem + 2 * 32 * TM + (buf * 32 + k) * TM; };
+    auto Bs = [&](int buf, int k) { return fg_smem + FG_NBUF * 32 * TM + (buf * 32 + k) * TM; };
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
     auto issue = [&](int kb, int buf) {
         const int kc = min(32, k1 - kb);
@@ -892,11 +894,13 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
     issue(k0, 0);
+    if (k0 + 32 < k1) issue(k0 + 32, 1);
     int buf = 0;
     for (int kb = k0; kb < k1; kb += 32) {
-        cp_async_wait_all();
-        __syncthreads();                 // chunk kb is in buffer buf; buf ^ 1 is free
-        if (kb + 32 < k1) issue(kb + 32, buf ^ 1);
+        if (kb + 32 < k1) cp_async_wait_one();   // this thread's copies of chunk kb have landed
+        else cp_async_wait_all();
+        __syncthreads();                 // chunk kb is in buffer buf; the buffer read before it is free
+        if (kb + 64 < k1) issue(kb + 64, (buf + 2) % FG_NBUF);
 #pragma unroll 8
         for (int k = 0; k < 32; ++k) {
             const float* ar = As(buf, k);
@@ -913,8 +917,7 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
 #pragma unroll
                 for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
         }
-        __syncthreads();                 // buffer buf may be overwritten next
-        buf ^= 1;
+        buf = (buf + 1) % FG_NBUF;
     }
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
@@ -1100,7 +1103,7 @@ __global__ void __launch_bounds__(256, 2) k_task_gemm_f32(const TriTask* __restr
     if (t.opB == OP_UPPER) ke = min(ke, j0 + TM);
     extern __shared__ __align__(16) float fg_smem[];
     auto As = [&](int buf, int k) { return fg_smem + (buf * 32 + k) * TM; };
-    auto Bs = [&](int buf, int k) { return fg_smem + 2 * 32 * TM + (buf * 32 + k) * TM; };
+    auto Bs = [&](int buf, int k) { return fg_smem + FG_NBUF * 32 * TM + (buf * 32 + k) * TM; };
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
     auto issue = [&](int k0c, int buf) {
 #pragma unroll 4
@@ -1139,12 +1142,14 @@ __global__ void __launch_bounds__(256, 2) k_task_gemm_f32(const TriTask* __restr
 #pragma unroll
         for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
     if (kb < ke) issue(kb, 0);
+    if (kb + 32 < ke) issue(kb + 32, 1);
     int buf = 0;
     for (int k0c = kb; k0c < ke; k0c += 32) {
-        cp_async_wait_all();
+        if (k0c + 32 < ke) cp_async_wait_one();
+        else cp_async_wait_all();
         unit_diag(k0c, buf);
         __syncthreads();
-        if (k0c + 32 < ke) issue(k0c + 32, buf ^ 1);
+        if (k0c + 64 < ke) issue(k0c + 64, (buf + 2) % FG_NBUF);
 #pragma unroll 8
         for (int k = 0; k < 32; ++k) {
             const float* ar = As(buf, k);
@@ -1161,8 +1166,7 @@ __global__ void __launch_bounds__(256, 2) k_task_gemm_f32(const TriTask* __restr
 #pragma unroll
                 for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
         }
-        __syncthreads();
-        buf ^= 1;
+        buf = (buf + 1) % FG_NBUF;
     }
     const float alpha = t.alpha;
 #pragma unroll
