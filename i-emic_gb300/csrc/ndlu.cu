@@ -1758,6 +1758,10 @@ NdLu::~NdLu() {
             cudaEventDestroy(r.a);
             cudaEventDestroy(r.b);
         }
+    for (cudaEvent_t e : fork_ev)
+        if (e) cudaEventDestroy(e);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     for (void* p : allocs) cudaFree(p);
 }
 
@@ -2113,7 +2117,13 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
         int maxnf = 0;
         for (int h = 0; h < plan.nlevels; ++h) maxnf = std::max(maxnf, plan.level_maxnf[h]);
         lu.subst = maxnf > subst_min_nf;
-        if (!lu.subst) lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
+        if (!lu.subst) {
+            lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
+            ck(cudaStreamCreateWithFlags(&lu.side, cudaStreamNonBlocking));
+            lu.fork_ev.assign(plan.nlevels, nullptr);
+            for (auto& e : lu.fork_ev) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ck(cudaEventCreateWithFlags(&lu.join_ev, cudaEventDisableTiming));
+        }
         lu.tri_flops = 0.0;
         for (const TriTask& t : tasks) lu.tri_flops += double(t.M) * t.N * t.K;   // ~ half are structural zeros
     }
@@ -2300,11 +2310,21 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
         const int gx = std::max(1, std::min(maxF, (152 * 16 + nfr - 1) / nfr));
         k_spill<T><<<dim3(gx, nfr), 256, 0, s>>>(lu.d_fronts, lf, front, factor, contrib); IEMIC_COUNT_LAUNCH();
         if (ev_sp) lu.timer->stop(ev_sp, s, IEMIC_KC_FACTOR_SETUP, 2.0 * sizeof(T) * double(P.level_work[h]), 0.0);
-        if (!lu.subst) {   // whole inverses of L11 / U11 in the factor store
-            cudaEvent_t ev2 = lu.timer ? lu.timer->start(s) : nullptr;
-            for (const auto& rg : lu.inv2_ranges[h]) tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_inv2_scratch), s);
-            if (ev2) lu.timer->stop(ev2, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
+        if (!lu.subst) {
+            // whole inverses of L11 / U11 in the factor store, on the side
+            // stream: they touch only this level's factors and their own
+            // scratch, so the next levels factor meanwhile
+            ck(cudaEventRecord(lu.fork_ev[h], s));
+            ck(cudaStreamWaitEvent(lu.side, lu.fork_ev[h], 0));
+            cudaEvent_t ev2 = lu.timer ? lu.timer->start(lu.side) : nullptr;
+            for (const auto& rg : lu.inv2_ranges[h])
+                tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_inv2_scratch), lu.side);
+            if (ev2) lu.timer->stop(ev2, lu.side, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
         }
+    }
+    if (!lu.subst) {   // the factorisation ends when the side stream has
+        ck(cudaEventRecord(lu.join_ev, lu.side));
+        ck(cudaStreamWaitEvent(s, lu.join_ev, 0));
     }
 }
 

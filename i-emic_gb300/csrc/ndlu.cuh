@@ -115,6 +115,11 @@ struct NdLu {
     int64_t inv2_scratch_entries = 0;
     void* d_inv2_scratch = nullptr;
     bool subst = false;                     // solves substitute over super-blocks (large fronts)
+    // the whole-inverse steps of a level run on a second stream (forked and
+    // joined inside the captured factorisation) while the next level factors
+    cudaStream_t side = nullptr;
+    std::vector<cudaEvent_t> fork_ev;       // per level
+    cudaEvent_t join_ev = nullptr;
     bool full_inverse = false;              // L11 / U11 replaced by their whole inverses
     double tri_flops = 0.0;
     cudaGraphExec_t factor_exec = nullptr;  // captured factorisation
