@@ -946,14 +946,14 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
 
 // write the inverted diagonal blocks (Linv_jj strict lower, Uinv_jj upper)
 template <class T, int B>
-__global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ front,
+__global__ void k_put_diag_inv(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, T* __restrict__ factor,
                                const T* __restrict__ dinv) {
     const FrontDev fr = fronts[lf[blockIdx.y]];
     const int nblk = (fr.nf + B - 1) / B;
     if (int(blockIdx.x) >= nblk) return;
     const int p = blockIdx.x * B, bb = min(B, fr.nf - p);
     const T* Di = dinv + fr.dinv_off + int64_t(blockIdx.x) * 2 * B * B;
-    T* A = front + fr.off;
+    T* A = factor + fr.foff;   // the first nf columns keep ld F in the factor store
     for (int e = threadIdx.x; e < bb * bb; e += blockDim.x) {
         int r = e / bb, c = e % bb;
         A[int64_t(p + c) * fr.F + p + r] = r > c ? Di[r * B + c] : Di[B * B + r * B + c];
@@ -2024,16 +2024,16 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
                                 const int64_t tcur = toff;
                                 toff += int64_t(na) * nd;
                                 if (!up && phase == 0)            // T = L21blk * Ainv   (nd x na)
-                                    emit(TriTask{fr.off + int64_t(a0) * F + d0, fr.off + int64_t(a0) * F + a0, tcur,
+                                    emit(TriTask{fr.foff + int64_t(a0) * F + d0, fr.foff + int64_t(a0) * F + a0, tcur,
                                                  F, F, nd, nd, na, na, OP_DENSE, OP_LOWER_UNIT, 0, 0, 1, 1.f});
                                 else if (!up)                     // X21 = -Dinv * T
-                                    emit(TriTask{fr.off + int64_t(d0) * F + d0, tcur, fr.off + int64_t(a0) * F + d0,
+                                    emit(TriTask{fr.foff + int64_t(d0) * F + d0, tcur, fr.foff + int64_t(a0) * F + d0,
                                                  F, nd, F, nd, na, nd, OP_LOWER_UNIT, OP_DENSE, 0, 1, 0, -1.f});
                                 else if (phase == 0)              // T = Ainv * U12blk   (na x nd)
-                                    emit(TriTask{fr.off + int64_t(a0) * F + a0, fr.off + int64_t(d0) * F + a0, tcur,
+                                    emit(TriTask{fr.foff + int64_t(a0) * F + a0, fr.foff + int64_t(d0) * F + a0, tcur,
                                                  F, F, na, na, nd, na, OP_UPPER, OP_DENSE, 0, 0, 1, 1.f});
                                 else                              // X12 = -T * Dinv
-                                    emit(TriTask{tcur, fr.off + int64_t(d0) * F + d0, fr.off + int64_t(d0) * F + a0,
+                                    emit(TriTask{tcur, fr.foff + int64_t(d0) * F + d0, fr.foff + int64_t(d0) * F + a0,
                                                  na, F, F, na, nd, nd, OP_DENSE, OP_UPPER, 1, 0, 0, -1.f});
                             }
                         }
@@ -2117,13 +2117,11 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
         int maxnf = 0;
         for (int h = 0; h < plan.nlevels; ++h) maxnf = std::max(maxnf, plan.level_maxnf[h]);
         lu.subst = maxnf > subst_min_nf;
-        if (!lu.subst) {
-            lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
-            ck(cudaStreamCreateWithFlags(&lu.side, cudaStreamNonBlocking));
-            lu.fork_ev.assign(plan.nlevels, nullptr);
-            for (auto& e : lu.fork_ev) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-            ck(cudaEventCreateWithFlags(&lu.join_ev, cudaEventDisableTiming));
-        }
+        if (!lu.subst) lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
+        ck(cudaStreamCreateWithFlags(&lu.side, cudaStreamNonBlocking));
+        lu.fork_ev.assign(plan.nlevels, nullptr);
+        for (auto& e : lu.fork_ev) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ck(cudaEventCreateWithFlags(&lu.join_ev, cudaEventDisableTiming));
         lu.tri_flops = 0.0;
         for (const TriTask& t : tasks) lu.tri_flops += double(t.M) * t.N * t.K;   // ~ half are structural zeros
     }
@@ -2298,34 +2296,30 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
                 fgemm(GM_TRAIL, dim3(tiles(maxF - P0) * tiles(maxF - P0), nfr), P0, P0);
             });
         }
-        // explicit inverses for the solve phase
-        const int maxblk = (maxnf + B - 1) / B;
-        cudaEvent_t ev_inv = lu.timer ? lu.timer->start(s) : nullptr;
-        k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, s>>>(lu.d_fronts, lf, front, dinv); IEMIC_COUNT_LAUNCH();
-        // merges inside the 256-row super-blocks: each diagonal super-block
-        // of L11 / U11 then holds its inverse, the solves substitute over them
-        for (const auto& rg : lu.tri_ranges[h]) tri_range<T>(lu, rg, front, static_cast<T*>(lu.d_tri_scratch), s);
-        if (ev_inv) lu.timer->stop(ev_inv, s, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
         cudaEvent_t ev_sp = lu.timer ? lu.timer->start(s) : nullptr;
         const int gx = std::max(1, std::min(maxF, (152 * 16 + nfr - 1) / nfr));
         k_spill<T><<<dim3(gx, nfr), 256, 0, s>>>(lu.d_fronts, lf, front, factor, contrib); IEMIC_COUNT_LAUNCH();
         if (ev_sp) lu.timer->stop(ev_sp, s, IEMIC_KC_FACTOR_SETUP, 2.0 * sizeof(T) * double(P.level_work[h]), 0.0);
-        if (!lu.subst) {
-            // whole inverses of L11 / U11 in the factor store, on the side
-            // stream: they touch only this level's factors and their own
-            // scratch, so the next levels factor meanwhile
-            ck(cudaEventRecord(lu.fork_ev[h], s));
-            ck(cudaStreamWaitEvent(lu.side, lu.fork_ev[h], 0));
-            cudaEvent_t ev2 = lu.timer ? lu.timer->start(lu.side) : nullptr;
+        // explicit inverses for the solve phase, in the factor store, on the
+        // side stream: they touch only this level's nf x nf blocks and their
+        // own scratch, so the next levels factor meanwhile. The inverted
+        // diagonal panel blocks, then merges inside the 256-row super-blocks
+        // (each diagonal super-block of L11 / U11 then holds its inverse), then
+        // for whole-inverse plans the row-oriented steps over the super-blocks.
+        ck(cudaEventRecord(lu.fork_ev[h], s));
+        ck(cudaStreamWaitEvent(lu.side, lu.fork_ev[h], 0));
+        cudaEvent_t ev_inv = lu.timer ? lu.timer->start(lu.side) : nullptr;
+        const int maxblk = (maxnf + B - 1) / B;
+        k_put_diag_inv<T, B><<<dim3(std::max(maxblk, 1), nfr), NT, 0, lu.side>>>(lu.d_fronts, lf, factor, dinv); IEMIC_COUNT_LAUNCH();
+        for (const auto& rg : lu.tri_ranges[h]) tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_tri_scratch), lu.side);
+        if (!lu.subst)
             for (const auto& rg : lu.inv2_ranges[h])
                 tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_inv2_scratch), lu.side);
-            if (ev2) lu.timer->stop(ev2, lu.side, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
-        }
+        if (ev_inv) lu.timer->stop(ev_inv, lu.side, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
     }
-    if (!lu.subst) {   // the factorisation ends when the side stream has
-        ck(cudaEventRecord(lu.join_ev, lu.side));
-        ck(cudaStreamWaitEvent(s, lu.join_ev, 0));
-    }
+    // the factorisation ends when the side stream's inverses are done
+    ck(cudaEventRecord(lu.join_ev, lu.side));
+    ck(cudaStreamWaitEvent(s, lu.join_ev, 0));
 }
 
 // The factorisation is a fixed sequence of ~1,400 launches over buffers that
