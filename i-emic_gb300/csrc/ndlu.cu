@@ -933,15 +933,12 @@ __global__ void __launch_bounds__(256, 2) k_fgemm_f32(const FrontDev* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// explicit inverses for the solve phase: after its LU, every front holds
-//   Linv11 (strict lower part, unit diagonal) and Uinv11 (upper part) in place
-//   of L11 and U11, so the triangular solves become dense GEMVs. FP32 factors
-//   also replace L21 by G = L21 * Linv11 and U12 by H = Uinv11 * U12, so both
-//   blocks of a sweep read the same input vector and one GEMV launch per
-//   level and sweep does the work (their solves run ~30 times per
-//   factorisation); FP64 factors keep L21 and U12 and run two dependent GEMV
-//   stages per level and sweep, because on GB300's FP64 pipe forming G and H
-//   costs more than the few extra launches of their handful of solves.
+// explicit inverses for the solve phase: after its LU, every front's 256-row
+//   diagonal super-blocks of L11 (strict lower part, unit diagonal) and U11
+//   (upper part) are replaced by their inverses; plans whose fronts stay at
+//   or below the substitution threshold then complete the whole inverses
+//   Linv11 / Uinv11, so the triangular solves become dense GEMVs. L21 and
+//   U12 are kept as they are (two dependent GEMV stages per level and sweep).
 // ---------------------------------------------------------------------------
 
 // write the inverted diagonal blocks (Linv_jj strict lower, Uinv_jj upper)
@@ -1077,7 +1074,7 @@ __global__ void __launch_bounds__(256) k_tri_gemm(const TriTask* __restrict__ ta
     }
 }
 
-// FP32 task GEMM (triangular inversion and G/H): C = alpha op(A) op(B) over
+// FP32 task GEMM (triangular inversion): C = alpha op(A) op(B) over
 // 128 x 128 tiles with the staging of k_fgemm_f32 (cp.async double buffering,
 // float4 operands, swizzled B). Masked triangular entries are zero-filled by
 // the copy; the implicit unit diagonal of OP_LOWER_UNIT operands is written
@@ -1214,14 +1211,12 @@ __global__ void k_expand(int ndim, const int* __restrict__ g2r, const char* __re
     }
 }
 
-// Solve phase, one level at a time (all fronts of the level together).
-// With L21/U12 (FP64 factors), two GEMV stages per level and sweep:
+// Solve phase, one level at a time (all fronts of the level together), two
+// GEMV stages per level and sweep:
 //   forward:  y = Linv11 (P w_own);           u_B = w_B - L21 y
 //   backward: t = y - U12 x_B;                x_own = Uinv11 t
-// With G/H (FP32 factors), one fused launch per level and sweep:
-//   forward:  y = Linv11 (P w_own), u_B = w_B - G (P w_own)
-//   backward: x_own = Uinv11 y - H x_B
-// Work items split every block into (256-row tile, 256-column chunk) pieces
+// (Linv11 / Uinv11 applied as whole inverses or by block substitution).
+// Work items split every block into (64-row tile, 256-column chunk) pieces
 // so the GEMVs spread over all SMs; partial sums per chunk are reduced in a
 // second pass (deterministic order), each stage into its own zero-initialised
 // buffer so that skipped empty tiles contribute exact zeros.
@@ -1539,8 +1534,8 @@ __global__ void k_bwd_gather(const FrontDev* __restrict__ fronts, const int* __r
 // ---------------------------------------------------------------------------
 // transposed solve phase (A^T y = c with the same factors; A = P^T L U per
 // front):
-//   leaves -> root: v_o = Uinv11^T c_o;  u_B = c_B - U12^T v_o  (G/H: - H^T c_o)
-//   root -> leaves: t = v_o - L21^T y_B; y_o = P^T Linv11^T t  (G/H: P^T (Linv11^T v_o - G^T y_B))
+//   leaves -> root: v_o = Uinv11^T c_o;  u_B = c_B - U12^T v_o
+//   root -> leaves: t = v_o - L21^T y_B; y_o = P^T Linv11^T t
 // Each stage reads one stored block column-wise: a warp owns a column, its
 // lanes stride down the rows (coalesced), and a tile of 64 columns x 256 rows
 // writes one partial sum per column.
@@ -1666,9 +1661,9 @@ __global__ void __launch_bounds__(NT) k_tfwd_gather(const FrontDev* __restrict__
     }
     WP[fr.woff + q] = w;
 }
-// leaves -> root epilogues. Two-stage: (UINV) v -> W[own], WP[own]; (U12)
-// W[B] = c_B + sums. Fused (H): both from the same launch.
-template <int MODE>   // 0: UINV only, 1: U12 only, 2: both (fused)
+// leaves -> root epilogues: MODE 0 (after UINV^T) v -> W[own], WP[own];
+// MODE 1 (after U12^T) W[B] = c_B + sums
+template <int MODE>
 __global__ void k_tfwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, TStageBufs sb,
                               double* __restrict__ W, double* __restrict__ WP) {
     const int f = lf[blockIdx.y];
@@ -1694,12 +1689,12 @@ __global__ void k_tbwd_gather(const FrontDev* __restrict__ fronts, const int* __
     if (q >= fr.F) return;
     WP[fr.woff + q] = q < fr.nf ? W[fr.woff + q] : yred[vars[fr.voff + q]];
 }
-// root -> leaves epilogues. MODE 0 (two-stage, after L21^T): WP[own] = v + sum;
-// MODE 1 (after LINV^T, or fused LINV^T + G^T): y_o = P^T (sum) scattered to yred
+// root -> leaves epilogues: MODE 0 (after L21^T) WP[own] = v + sum;
+// MODE 1 (after LINV^T) y_o = P^T (sum) scattered to yred
 template <int MODE>
 __global__ void k_tbwd_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, TStageBufs sb,
                               const int* __restrict__ piv, double* __restrict__ WP, double* __restrict__ yred,
-                              int fused, int B) {
+                              int B) {
     const int f = lf[blockIdx.y];
     const FrontDev fr = fronts[f];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1707,9 +1702,7 @@ __global__ void k_tbwd_reduce(const FrontDev* __restrict__ fronts, const int* __
     if (MODE == 0) {
         WP[fr.woff + q] += tstage_sum(TS_L21, f, fr, q, sb);
     } else {
-        double y = tstage_sum(TS_LINV, f, fr, q, sb);
-        if (fused && fr.nb > 0) y += tstage_sum(TS_L21, f, fr, q, sb);
-        yred[fr.red0 + piv_row(piv, fr, q, B)] = y;
+        yred[fr.red0 + piv_row(piv, fr, q, B)] = tstage_sum(TS_LINV, f, fr, q, sb);
     }
 }
 // reduced transposed right-hand side: column-scaled wet entries
@@ -1783,8 +1776,6 @@ static void* dmalloc(NdLu& lu, size_t bytes) {
 
 void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
     cudaStream_t s = 0;
-    ck(cudaFuncSetAttribute(k_fgemm_f32<GM_STRIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
-    ck(cudaFuncSetAttribute(k_fgemm_f32<GM_BAND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     ck(cudaFuncSetAttribute(k_fgemm_f32<GM_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     ck(cudaFuncSetAttribute(k_task_gemm_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(FG_SMEM)));
     lu.prec = prec;
@@ -1858,9 +1849,8 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
     lu.d_cmax = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(plan.ndim)));
     lu.d_npert = static_cast<int*>(dmalloc(lu, 2 * sizeof(int)));
     lu.d_wp = dmalloc(lu, sizeof(double) * size_t(plan.w_entries));
-    // solve-phase partial-sum buffers (per stage) and work items (per launch
-    // group: G/H layout fuses LINV+L21 and UINV+U12; the L21/U12 layout runs
-    // the four stages as separate groups)
+    // solve-phase partial-sum buffers (per stage) and work items (one launch
+    // group per stage)
     std::vector<WorkItem> items[NSTAGE];
     for (int st = 0; st < NSTAGE; ++st) {
         std::vector<int64_t> off(plan.nfronts, 0);
@@ -1950,8 +1940,7 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
         lu.d_sub_part = static_cast<double*>(dmalloc(lu, sizeof(double) * size_t(std::max<int64_t>(pmax, 1))));
     }
     // transposed solve: partial buffers per stage (columns x row chunks) and
-    // work items per launch group: G/H layout fuses UINV^T+H^T (group 0) and
-    // LINV^T+G^T (group 3); the L21/U12 layout runs four separate groups
+    // work items, one launch group per stage
     for (int st = 0; st < 4; ++st) {
         std::vector<int64_t> off(plan.nfronts, 0);
         int64_t poff = 0;
@@ -2579,9 +2568,9 @@ static void apply_transpose_t(NdLu& lu, const TV* r, TV* z, cudaStream_t s) {
         const dim3 gF((P.level_maxF[h] + NT - 1) / NT, nfr), gN((P.level_maxnf[h] + NT - 1) / NT, nfr);
         k_tbwd_gather<<<gF, NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
         launch_tgroup<T>(lu, 2, h, front, WP, s);   // -L21^T y_B
-        k_tbwd_reduce<0><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
+        k_tbwd_reduce<0><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, B); IEMIC_COUNT_LAUNCH();
         launch_tgroup<T>(lu, 3, h, front, WP, s);   // LINV^T t
-        k_tbwd_reduce<1><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, 0, B); IEMIC_COUNT_LAUNCH();
+        k_tbwd_reduce<1><<<gN, NT, 0, s>>>(lu.d_fronts, lf, sb, lu.d_piv, WP, red, B); IEMIC_COUNT_LAUNCH();
     }
     k_texpand<TV><<<blocks_for(P.ndim), NT, 0, s>>>(P.ndim, lu.d_g2r, lu.d_isdry, lu.d_dr, red, r, z); IEMIC_COUNT_LAUNCH();
     ck(cudaGetLastError());
