@@ -411,6 +411,53 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
         plan.asm_row[d] = ent_r[e];
         plan.asm_dst[d] = ent_dst[e];
     }
+    check_nd_plan(plan);
+}
+
+// Every offset and index the numeric kernels derive from the plan stays
+// inside its buffer: fronts in the working area of their level, the factor
+// store and the contribution ring, solve vectors, inverse panel blocks,
+// extend-add maps in the parent, assembly targets, the reduced ordering.
+// Throws IEMIC_ERR_STATE otherwise.
+void check_nd_plan(const NdPlan& P) {
+    auto req = [](bool ok) {
+        if (!ok) throw EngineError(IEMIC_ERR_STATE);
+    };
+    int64_t fsum = 0;
+    int roots = 0;
+    req(int(P.fronts.size()) == P.nfronts && int(P.level_work.size()) == P.nlevels);
+    req(int(P.asm_level_start.size()) == P.nlevels + 1 && P.contrib_ring >= 1);
+    for (int q = 0; q < P.nfronts; ++q) {
+        const FrontDev& fr = P.fronts[q];
+        req(fr.nf >= 0 && fr.nb >= 0 && fr.F == fr.nf + fr.nb && fr.lvl >= 0 && fr.lvl < P.nlevels);
+        req(fr.foff == fsum);
+        fsum += int64_t(fr.nf) * fr.nf + 2 * int64_t(fr.nf) * fr.nb;
+        req(fr.off >= 0 && fr.off + int64_t(fr.F) * fr.F <= P.level_work[fr.lvl]);
+        req(P.level_work[fr.lvl] <= P.work_entries);
+        req(fr.soff >= 0 && fr.soff + int64_t(fr.nb) * fr.nb <= int64_t(P.contrib_ring) * P.contrib_slot_entries);
+        req(fr.red0 >= 0 && fr.red0 + fr.nf <= P.nred);
+        req(fr.voff >= 0 && fr.voff + fr.F <= int64_t(P.vars.size()));
+        for (int a = 0; a < fr.F; ++a) req(P.vars[fr.voff + a] >= 0 && P.vars[fr.voff + a] < P.nred);
+        req(fr.woff >= 0 && fr.woff + fr.F <= P.w_entries);
+        req(fr.dinv_off + int64_t((fr.nf + P.panel - 1) / P.panel) * 2 * P.panel * P.panel <= P.dinv_entries);
+        if (fr.parent >= 0) {
+            req(fr.parent < P.nfronts);
+            const FrontDev& pa = P.fronts[fr.parent];
+            req(pa.lvl > fr.lvl && pa.lvl - fr.lvl < P.contrib_ring);
+            req(fr.emap_off >= 0 && fr.emap_off + fr.nb <= int64_t(P.emap.size()));
+            for (int a = 0; a < fr.nb; ++a) req(P.emap[fr.emap_off + a] >= 0 && P.emap[fr.emap_off + a] < pa.F);
+        } else {
+            req(fr.nb == 0);
+            ++roots;
+        }
+    }
+    req(roots == 1 && fsum == P.factor_entries);
+    for (int h = 0; h < P.nlevels; ++h)
+        for (int64_t d = P.asm_level_start[h]; d < P.asm_level_start[h + 1]; ++d)
+            req(P.asm_dst[d] >= 0 && P.asm_dst[d] < P.level_work[h]);
+    req(int(P.r2g.size()) == P.nred && int(P.g2r.size()) == P.ndim);
+    for (int q = 0; q < P.nred; ++q) req(P.r2g[q] >= 0 && P.r2g[q] < P.ndim && P.g2r[P.r2g[q]] == q);
+    req(int(P.dry_ptr.size()) == P.nred + 1);
 }
 
 // ===========================================================================

@@ -55,6 +55,8 @@ struct NdPlan {
     int64_t factor_entries = 0;     // entries the solve phase reads
 };
 
+// consistency of a plan's offsets and indices (throws IEMIC_ERR_STATE)
+void check_nd_plan(const NdPlan& plan);
 void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::vector<int>& landm,
                    const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel);
 

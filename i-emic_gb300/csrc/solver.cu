@@ -155,6 +155,33 @@ int iemic_get_fronts(iemic_ocean* h, int cap, int* nf, int* nb, int* level, int*
     GUARD_END
 }
 
+int iemic_analyse_pattern(const iemic_config* cfg, const int* landm, const int* row_ptr, const int* col_idx,
+                          iemic_solver_info* out) {
+    if (!cfg || !landm || !row_ptr || !col_idx || !out || cfg->n < 1 || cfg->m < 1 || cfg->l < 1)
+        return IEMIC_ERR_ARG;
+    GUARD_BEGIN
+    const int64_t ndim = int64_t(6) * cfg->n * cfg->m * cfg->l;
+    const int64_t nmask = int64_t(cfg->n + 2) * (cfg->m + 2) * (cfg->l + 2);
+    if (ndim > INT32_MAX || row_ptr[0] != 0 || row_ptr[ndim] < 0) return IEMIC_ERR_ARG;
+    std::vector<int> lm(landm, landm + nmask), rp(row_ptr, row_ptr + ndim + 1), ci(col_idx, col_idx + row_ptr[ndim]);
+    for (int64_t r = 0; r < ndim; ++r)
+        if (rp[r + 1] < rp[r]) return IEMIC_ERR_ARG;
+    for (int c : ci)
+        if (c < 0 || c >= ndim) return IEMIC_ERR_ARG;
+    NdPlan P;
+    build_nd_plan(P, cfg->n, cfg->m, cfg->l, cfg->periodic ? 1 : 0, lm, rp, ci, 32);   // checks the plan
+    out->unknowns = P.ndim;
+    out->reduced_unknowns = P.nred;
+    out->fronts = P.nfronts;
+    out->levels = P.nlevels;
+    out->factor_entries = P.factor_entries;
+    out->front_entries = P.front_entries;
+    out->factor_flops = P.flops;
+    out->work_entries = P.work_entries;
+    out->contrib_entries = int64_t(P.contrib_ring) * P.contrib_slot_entries;
+    GUARD_END
+}
+
 int iemic_kernel_timing(iemic_ocean* h, int enable) {
     if (!h) return IEMIC_ERR_ARG;
     GUARD_BEGIN

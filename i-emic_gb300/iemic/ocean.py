@@ -179,6 +179,7 @@ SIGNATURES = {
     "iemic_launch_count": [],
     "iemic_kernel_timing_failures": [_VP],
     "iemic_set_substitution_threshold": [_VP, ctypes.c_int],
+    "iemic_analyse_pattern": [ctypes.POINTER(Config), _IP, _IP, _IP, ctypes.POINTER(SolverInfo)],
     "iemic_get_fronts": [_VP, ctypes.c_int, _IP, _IP, _IP, _IP, _IP],
     "iemic_kernel_trace": [_VP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float), _DP, _IP],
 }
@@ -215,6 +216,23 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(_IP)
+
+
+def analyse_pattern(cfg, landm, row_ptr, col_idx):
+    """Host-side symbolic analysis of the preconditioner for a grid, the
+    engine's land mask and J's 0-based CSR pattern (no GPU needed): the size
+    report of iemic_get_solver_info, after the plan's consistency checks."""
+    L = load_library()
+    lm = np.ascontiguousarray(landm, dtype=np.int32)
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+    st = SolverInfo()
+    rc = L.iemic_analyse_pattern(ctypes.byref(Config(**{k: cfg[k] for k, _ in Config._fields_})),
+                                 lm.ctypes.data_as(_IP), rp.ctypes.data_as(_IP), ci.ctypes.data_as(_IP),
+                                 ctypes.byref(st))
+    if rc != 0:
+        raise IemicError(rc, "analyse_pattern")
+    return _asdict(st)
 
 
 class Ocean:

@@ -157,6 +157,13 @@ typedef struct {
     int64_t work_entries, contrib_entries;
 } iemic_solver_info;
 int iemic_get_solver_info(iemic_ocean* h, iemic_solver_info* out);
+/* The same size report from the host-side symbolic analysis alone (no device
+ * work, no handle): grid from cfg (n, m, l, periodic), the land mask as the
+ * engine holds it ((n+2)(m+2)(l+2) entries, iemic_get_landm) and the 0-based
+ * CSR pattern of J (row_ptr: 6nml + 1 entries). The plan's offsets and maps
+ * are checked for consistency; IEMIC_ERR_STATE if one fails. */
+int iemic_analyse_pattern(const iemic_config* cfg, const int* landm, const int* row_ptr, const int* col_idx,
+                          iemic_solver_info* out);
 /* Triangular solves of the preconditioner: a factorisation whose fronts have
  * at most `max_inverse_nf` own unknowns (default 12288) stores the whole
  * inverses of their diagonal triangles and applies them as GEMVs; a larger one
