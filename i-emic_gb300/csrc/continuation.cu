@@ -14,8 +14,11 @@
 //    Ocean::preProcess (src/ocean/Ocean.C:799-808) asks for a new
 //    preconditioner at the start of each step; the next solve builds it and
 //    the rest of the step reuses it.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <functional>
 
 #include "engine.cuh"
@@ -56,16 +59,35 @@ struct DevVecs {
 
 // The model side of the drivers: F, J and solves with the reference's
 // preconditioner policy, plus timing.
+//
+// Preconditioner policy (`policy`):
+//  0  rebuilt once per continuation step (Ocean::preProcess,
+//     src/ocean/Ocean.C:799-808) and reused for every later Jacobian of the step;
+//  1  rebuilt after every new Jacobian;
+//  2  as 0, plus a cost-balanced rebuild: a factorisation is reused while the
+//     Krylov time spent beyond the iteration count of its first solve stays
+//     below the time the factorisation itself took (the break-even rule of
+//     rent-or-buy); once it exceeds it, the next solve refactors the current
+//     Jacobian. The same budget caps a solve that runs on the factors of an
+//     older Jacobian: when it is spent before the solve converges, the solve
+//     is repeated on a fresh factorisation of the current Jacobian.
 struct ModelOps {
     Engine& e;
     iemic_solve_opts solve_opts;
-    bool refactor_each = false;
+    int policy = 0;
     bool recompute = true;   // set by pre_process
     long jac_gen = 0, fact_gen = -1;
     double t_asm = 0, t_fac = 0, t_sol = 0;
-    int solves = 0, krylov = 0, facts = 0, unconverged = 0;
+    int solves = 0, krylov = 0, facts = 0, unconverged = 0, retries = 0;
+    double fact_ms = 0.0, excess_ms = 0.0;   // cost of the current factorisation, Krylov time beyond its first solve
+    int base_iters = 0;                      // iterations of the first solve on the current factorisation
+    double iter_ms = 0.0;                    // time of one Krylov iteration, from the last solve
+    bool trace = false;
 
-    ModelOps(Engine& en, const iemic_solve_opts& o, bool each) : e(en), solve_opts(o), refactor_each(each) {}
+    ModelOps(Engine& en, const iemic_solve_opts& o, int pol) : e(en), solve_opts(o), policy(pol) {
+        const char* t = std::getenv("IEMIC_SOLVE_TRACE");
+        trace = t && *t && *t != '0';
+    }
     void rhs(const double* x, double* F) {
         auto t = clk::now();
         e.rhs_dev(x, F);
@@ -80,23 +102,49 @@ struct ModelOps {
         ++jac_gen;
     }
     void pre_process() { recompute = true; }
-    void solve(const double* b, double* x) {
-        const bool need = recompute || (refactor_each && fact_gen != jac_gen);
+    int solve_once(const double* b, double* x, bool refactor, int cap) {
         iemic_solve_opts o = solve_opts;
-        o.reuse_preconditioner = need ? 0 : 1;
+        o.reuse_preconditioner = refactor ? 0 : 1;
+        if (cap > 0 && cap < o.max_iters) o.max_iters = cap;
         iemic_solve_stats st{};
         int rc = e.solve_dev(b, x, o, st);
         if (rc != IEMIC_OK && rc != IEMIC_ERR_NOT_CONVERGED) throw EngineError(rc);
-        if (rc == IEMIC_ERR_NOT_CONVERGED) ++unconverged;
-        if (need) {
+        if (refactor) {
             recompute = false;
             fact_gen = jac_gen;
         }
+        if (st.factorizations > 0) {
+            fact_ms = st.time_factor_ms;
+            base_iters = st.iters;
+            excess_ms = 0.0;
+        } else if (st.iters > base_iters) {
+            excess_ms += double(st.iters - base_iters) * st.time_solve_ms / double(st.iters);
+        }
+        if (st.iters > 0) iter_ms = st.time_solve_ms / double(st.iters);
         t_fac += st.time_factor_ms;
         t_sol += st.time_solve_ms;
         ++solves;
         krylov += st.iters;
         facts += st.factorizations;
+        if (trace)
+            std::fprintf(stderr, "iemic solve: jac %ld fact %ld iters %d relres %.3e factor_ms %.1f solve_ms %.1f%s\n",
+                         jac_gen, fact_gen, st.iters, st.relres, st.time_factor_ms, st.time_solve_ms,
+                         rc == IEMIC_OK ? "" : " NOT CONVERGED");
+        return rc;
+    }
+    void solve(const double* b, double* x) {
+        const bool newer = fact_gen != jac_gen;
+        const bool need = recompute || (policy == 1 && newer) || (policy == 2 && newer && excess_ms >= fact_ms);
+        const bool stale = policy == 2 && !need && newer;
+        int cap = 0;
+        if (stale && iter_ms > 0.0)   // iterations the remaining rebuild budget pays for
+            cap = base_iters + std::max(10, int(std::ceil((fact_ms - excess_ms) / iter_ms)));
+        int rc = solve_once(b, x, need, cap);
+        if (rc == IEMIC_ERR_NOT_CONVERGED && stale) {
+            ++retries;
+            rc = solve_once(b, x, true, 0);
+        }
+        if (rc == IEMIC_ERR_NOT_CONVERGED) ++unconverged;
     }
     double dot(const double* a, const double* b) { return dev_dot(e, a, b); }
     double norm(const double* a) { return std::sqrt(dev_dot(e, a, a)); }
@@ -362,10 +410,16 @@ struct Continuation {
             ++step;
             store();
             if (do_step()) {
+                if (M.trace)
+                    std::fprintf(stderr, "iemic step %d FAILED: par %.9g newton %d res %.3e\n", step, par,
+                                 newton_iter, last_res);
                 reset();
                 ++failed;
                 continue;
             }
+            if (M.trace)
+                std::fprintf(stderr, "iemic step %d: par %.9g ds %.3e newton %d res %.3e\n", step, par, ds,
+                             newton_iter, last_res);
             detect();
             adjust_step();
         }
@@ -406,7 +460,7 @@ int iemic_newton_dev(iemic_ocean* h, double* x, const iemic_newton_opts* opts, i
     try {
         DevVecs V(e, 3);
         double *F = V.v[0], *dx = V.v[1], *b = V.v[2];
-        ModelOps M(e, o.solve, o.refactor_each_iter != 0);
+        ModelOps M(e, o.solve, o.refactor_each_iter);
         M.rhs(x, F);
         double norm_rhs = M.norm(F), test = norm_rhs;
         s.rhs_norm0 = norm_rhs;
@@ -522,7 +576,7 @@ int iemic_continuation_run_dev(iemic_ocean* h, double* x, const iemic_continuati
     auto t0 = clk::now();
     try {
         DevVecs V(e, 10);
-        ModelOps M(e, o.solve, o.refactor_each_newton != 0);
+        ModelOps M(e, o.solve, o.refactor_each_newton);
         Continuation C(M, o, x, V);
         C.run(s);
         if (C.abort_flag) rc = IEMIC_ERR_NOT_CONVERGED;

@@ -47,6 +47,11 @@ struct Engine {
     int8_t* d_slot = nullptr;
     double *d_jt = nullptr, *d_kt = nullptr, *d_al = nullptr, *d_pads = nullptr, *d_surf = nullptr;
     double *d_x = nullptr, *d_F = nullptr, *d_v1 = nullptr, *d_v2 = nullptr, *d_B = nullptr;
+    int device = 0;           // the CUDA device the handle was created on
+    // vertical mixing (Mixing >= 1): partition flags (device) and norm partials
+    int* d_mixflags = nullptr;
+    double* d_mixpart = nullptr;
+    int any_ocean = 0;
     int *d_rowptr = nullptr, *d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
@@ -78,6 +83,11 @@ struct Engine {
     void set_par(int idx, double value);
     void rhs_dev(const double* x, double* F);
     void jacobian_dev(const double* x);
+    // mixing scalars of the current parameters; throws IEMIC_ERR_ARG for the
+    // neutral-physics / Gent-McWilliams terms, which have no GPU kernels
+    MixParams mix_params() const;
+    // vmix_control before an rhs or jacobian (Mixing = 2); part: 2*152 doubles
+    void mix_control(const double* x, double* part);
 
     // linear algebra (krylov.cu)
     void spmv64(const double* x, double* y);

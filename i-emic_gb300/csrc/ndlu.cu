@@ -82,6 +82,14 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
     //    are pinned, as THCM's fixPressurePoints rows would pin them
     //    (src/ocean/THCM.C:2260-2297): this removes the constant and
     //    checkerboard null modes of J from the preconditioner.
+    //    The B-grid gradient at an active velocity point vanishes exactly when
+    //    the two diagonal pairs of its four columns carry equal pressures, so
+    //    the null modes are the functions constant on the components of the
+    //    "diagonal" graph (edges (i,j)-(i+1,j+1) and (i+1,j)-(i,j+1) per active
+    //    point). A basin usually splits into two such components (constant and
+    //    checkerboard); where a region hangs on through a single velocity point
+    //    its checkerboard is separate, and any component the adjacent pair
+    //    leaves unpinned gets a pin of its own.
     std::vector<char> ocean_col(size_t(n) * m, 0), uv_col(size_t(n) * m, 0);
     for (int j = 0; j < m; ++j)
         for (int i = 0; i < n; ++i) {
@@ -107,6 +115,30 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
                     uf[find(i + n * j)] = find(ii + n * jj);
                 }
             }
+        // diagonal components
+        std::vector<int> dg(size_t(n) * m);
+        std::iota(dg.begin(), dg.end(), 0);
+        std::function<int(int)> dfind = [&](int a) {
+            while (dg[a] != a) { dg[a] = dg[dg[a]]; a = dg[a]; }
+            return a;
+        };
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < n; ++i) {
+                int ie = i + 1;
+                if (periodic) ie %= n;
+                if (ie >= n || j + 1 >= m) continue;
+                bool active = false;
+                for (int k = 0; k < l && !active; ++k) active = !dry[grow(i, j, k, 0)];
+                if (!active) continue;
+                dg[dfind(i + n * j)] = dfind(ie + n * (j + 1));
+                dg[dfind(ie + n * j)] = dfind(i + n * (j + 1));
+            }
+        std::vector<char> dpinned(size_t(n) * m, 0);
+        auto pin = [&](int c) {
+            if (dpinned[dfind(c)]) return;
+            dpinned[dfind(c)] = 1;
+            plan.pins.push_back(grow(c % n, c / n, l - 1, PP - 1));
+        };
         std::vector<std::vector<int>> comps(size_t(n) * m);
         for (int j = m - 1; j >= 0; --j)      // scan from the north-east corner
             for (int i = n - 1; i >= 0; --i)
@@ -119,8 +151,8 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
             for (int c : K) {   // a horizontally adjacent pair first
                 int i = c % n, j = c / n, iw = periodic ? (i - 1 + n) % n : i - 1;
                 if (iw >= 0 && in[iw + n * j]) {
-                    plan.pins.push_back(grow(i, j, l - 1, PP - 1));
-                    plan.pins.push_back(grow(iw, j, l - 1, PP - 1));
+                    pin(c);
+                    pin(iw + n * j);
                     done = true;
                     break;
                 }
@@ -128,12 +160,13 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
             for (size_t q = 0; q < K.size() && !done; ++q) {
                 int i = K[q] % n, j = K[q] / n;
                 if (j > 0 && in[i + n * (j - 1)]) {
-                    plan.pins.push_back(grow(i, j, l - 1, PP - 1));
-                    plan.pins.push_back(grow(i, j - 1, l - 1, PP - 1));
+                    pin(K[q]);
+                    pin(i + n * (j - 1));
                     done = true;
                 }
             }
-            if (!done) plan.pins.push_back(grow(K[0] % n, K[0] / n, l - 1, PP - 1));
+            if (!done) pin(K[0]);
+            for (int c : K) pin(c);   // components the pair left unpinned
         }
         for (int p : plan.pins) dry[p] = 1;
     }

@@ -136,10 +136,12 @@ void Engine::build_grid() {
         K(KT_DFZT, k) = dfzT[k];
         K(KT_ZHDIM, k) = z[k] * cfg.hdim;
     }
+    for (int k = 0; k <= l; ++k) K(KT_DFZW, k) = dfzW[k];
     tdzi2 = 1.0 / (2 * dz);
 }
 
-// stpnt (src/ocean/usrc.F90:1153-1197) with vmix_par for Mixing = 0
+// stpnt (src/ocean/usrc.F90:1153-1197); vmix_par (src/ocean/mix_imp.f:113-128)
+// clears MIXP, P_VC, MKAP only for Mixing = 0
 void Engine::stpnt() {
     double* p = P.par;
     for (int i = 0; i <= NPAR; ++i) p[i] = 0.0;
@@ -157,6 +159,7 @@ void Engine::stpnt() {
     p[ENER] = 1.0e+02;
     p[SPL1] = 2.0e+03;
     p[SPL2] = 0.01;
+    if (cfg.vmix != 0) p[P_VC] = 2.5e+04 * p[PE_V];
     P.TRES = cfg.tres;
     P.SRES = cfg.sres;
 }
@@ -264,6 +267,7 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
     const int n = c.n, m = c.m, l = c.l;
     nc = size_t(n) * m * l;
     ndim = int(NUN * nc);
+    ck(cudaGetDevice(&device));
     ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     // land mask as src/ocean/usrc.F90:79-107 leaves it
     const size_t nl = size_t(n + 2) * (m + 2) * (l + 2);
@@ -327,7 +331,37 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
     lin();
     launch_mass(geo, P, d_B, stream);
     ck(cudaGetLastError());
+    // vmix_init (src/ocean/mix_imp.f:57-111): Mixing = 1 fixes the partition
+    // of T and S rows and columns; Mixing = 2 starts with both fields off
+    for (int k = 1; k <= l && !any_ocean; ++k)
+        for (int j = 1; j <= m && !any_ocean; ++j)
+            for (int i = 1; i <= n && !any_ocean; ++i) any_ocean = LM(i, j, k) == OCEAN ? 1 : 0;
+    int flags[5] = {0, 0, 0, 0, 0};
+    if (c.vmix == 1) { flags[0] = flags[1] = flags[2] = flags[3] = 1; flags[4] = any_ocean; }
+    d_mixflags = static_cast<int*>(dalloc(sizeof(flags)));
+    d_mixpart = static_cast<double*>(dalloc(sizeof(double) * 2 * 152));
+    ck(cudaMemcpyAsync(d_mixflags, flags, sizeof(flags), cudaMemcpyHostToDevice, stream));
     ck(cudaStreamSynchronize(stream));
+}
+
+MixParams Engine::mix_params() const {
+    MixParams M{};
+    M.on = (cfg.vmix == 1 || cfg.vmix == 2) ? 1 : 0;
+    if (M.on && (P.par[MIXP] != 0.0 || P.par[MKAP] != 0.0)) throw EngineError(IEMIC_ERR_ARG);
+    M.rhomix = (cfg.rho_mixing != 0 && P.par[NLES] == 0.0) ? 1 : 0;
+    M.lambda = P.par[LAMB];
+    M.xes = P.par[NLES];
+    M.kvc = P.par[P_VC];
+    M.eps = (1.0 - P.par[ALPC]) * P.par[ENER] * P.par[PE_V];
+    M.fac = cfg.alphaT * P.par[SPL1];
+    M.flags = d_mixflags;
+    return M;
+}
+
+// Ocean::computeRHS / computeJacobian call THCM::fixMixing(0) (Ocean.C:1281,
+// 1302), so with Mixing = 2 every evaluation re-runs vmix_control.
+void Engine::mix_control(const double* x, double* part) {
+    if (cfg.vmix == 2) launch_mix_control(geo, x, part, d_mixflags, any_ocean, stream);
 }
 
 void Engine::set_par(int idx, double value) {
@@ -343,17 +377,21 @@ void Engine::set_par(int idx, double value) {
 // back (usol), plus the residual (3 vectors) or the CSR values written (FP64
 // and FP32 copies) for the Jacobian.
 void Engine::rhs_dev(const double* x, double* F) {
+    const MixParams mp = mix_params();
     cudaEvent_t ev = timer.start(stream);
     launch_usol(geo, x, d_pads, stream);
-    launch_rhs(geo, P, fs, d_al, d_pads, x, d_surf, F, stream);
+    mix_control(x, d_mixpart);
+    launch_rhs(geo, P, mp, fs, d_al, d_pads, x, d_surf, F, stream);
     timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 8.0 * 4.0 * ndim, 0.0);
     ck(cudaGetLastError());
 }
 
 void Engine::jacobian_dev(const double* x) {
+    const MixParams mp = mix_params();
     cudaEvent_t ev = timer.start(stream);
     launch_usol(geo, x, d_pads, stream);
-    launch_jacobian(geo, P, pat, d_al, d_pads, d_val, d_val32, stream);
+    mix_control(x, d_mixpart);
+    launch_jacobian(geo, P, mp, pat, d_al, d_pads, d_val, d_val32, stream);
     timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 12.0 * double(nnz) + 8.0 * 3.0 * ndim, 0.0);
     ck(cudaGetLastError());
     jac_valid = true;

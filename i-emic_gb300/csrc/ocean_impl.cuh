@@ -25,7 +25,7 @@ enum JTab {   // per latitude row j = 0..m+1
 };
 enum KTab {   // per level k = 0..l+1
     KT_UZZ14, KT_UZZ23, KT_PZ5, KT_PZ23, KT_WZC5, KT_WZC14, KT_TZZ14, KT_TZZ23,
-    KT_TDZ8, KT_DFZT, KT_ZHDIM,
+    KT_TDZ8, KT_DFZT, KT_ZHDIM, KT_DFZW,
     NKT
 };
 
@@ -48,6 +48,17 @@ struct Geo {
 struct Params {
     double par[NPAR + 1];
     int TRES, SRES;
+};
+
+// Vertical mixing and convective adjustment (src/ocean/mix_imp.f vmix_fun,
+// Mixing >= 1): scalars of one call, and the device-resident state of the
+// adaptive partition, flags[5] = {vmix_temp, vmix_salt, partition rows/columns
+// T, partition rows/columns S, partition built (vmix_dim > 0)}.
+struct MixParams {
+    int on;                     // Mixing >= 1
+    int rhomix;                 // Rho Mixing and a linear equation of state
+    double lambda, xes, kvc, eps, fac;   // LAMB, NLES, P_VC, (1-ALPC) ENER PE_V, alphaT SPL1
+    const int* flags;
 };
 
 // Scalars of the forcing routine (src/ocean/forcing.F90:4-218) for the
@@ -74,10 +85,13 @@ void launch_lin(const Geo& g, const Params& p, double* al_tab, cudaStream_t s);
 void launch_usol(const Geo& g, const double* x, double* pads, cudaStream_t s);
 void launch_dfdsurf_t(const Geo& g, const ForcingScalars& fs, const double* lambda, double* grad, cudaStream_t s);
 void launch_pattern(const Geo& g, const Pattern& pat, int* col_idx, cudaStream_t s);
-void launch_jacobian(const Geo& g, const Params& p, const Pattern& pat, const double* al_tab,
+void launch_jacobian(const Geo& g, const Params& p, const MixParams& mp, const Pattern& pat, const double* al_tab,
                      const double* pads, double* val, float* val32, cudaStream_t s);
-void launch_rhs(const Geo& g, const Params& p, const ForcingScalars& fs, const double* al_tab,
+void launch_rhs(const Geo& g, const Params& p, const MixParams& mp, const ForcingScalars& fs, const double* al_tab,
                 const double* pads, const double* x, const double* surf, double* F, cudaStream_t s);
+// vmix_control (src/ocean/mix_imp.f:131-166) on the device: ||T||_2, ||S||_2
+// of the state (part: 2 * 152 doubles of scratch) and the flag update.
+void launch_mix_control(const Geo& g, const double* x, double* part, int* flags, int any_ocean, cudaStream_t s);
 void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s);
 
 }  // namespace iemic

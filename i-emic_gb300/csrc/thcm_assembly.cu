@@ -357,6 +357,221 @@ __device__ __forceinline__ double an_rhs(double al, int kk, const Cell& c, const
 }
 
 // ---------------------------------------------------------------------------
+// Vertical mixing and convective adjustment (src/ocean/mix_imp.f, Mixing >= 1)
+// of one water column: the implicit vertical mixing Ftimp/Fsimp (P_VC) and
+// the consistent vertical mixing Ftzt/Fszt (ALPC < 1) at the top faces
+// k-1 and k of cell (i,j,k), and the T/S divergence terms of vmix_fun
+// (mix_imp.f:231-562) in its operation order. The horizontal neutral-physics
+// and Gent-McWilliams fluxes are zero (MIXP = MKAP = 0, checked on the host),
+// so their two divergence stages leave mix(row) = +0.0 exactly.
+// ---------------------------------------------------------------------------
+// tanh by one explicit algorithm, shared operation for operation with the
+// oracle (the platform tanh's last bit is implementation-defined): |y| < 2^-27
+// gives y, |y| > 22 gives +-1, otherwise e/(e+2) with e = expm1(2|y|) from a
+// degree-13 Taylor series, after Cody-Waite reduction by ln2 above ln2/2.
+__device__ __forceinline__ double expm1_taylor(double r) {
+    const double c[13] = {0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26,
+                          0x1.27e4fb7789f5cp-22, 0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16,
+                          0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7,
+                          0x1.5555555555555p-5,  0x1.5555555555555p-3,  0x1.0p-1,
+                          0x1.0p+0};   // 1/13!, ..., 1/1!
+    double p = c[0];
+#pragma unroll
+    for (int q = 1; q < 13; ++q) p = p * r + c[q];
+    return p * r;
+}
+__device__ __forceinline__ double tanh_x(double y) {
+    const double a = fabs(y);
+    if (!(a >= 0x1p-27)) return y;
+    if (a > 22.0) return y > 0 ? 1.0 : -1.0;
+    const double x = 2.0 * a;
+    double e;
+    if (x <= 0x1.62e42fefa39efp-2) {
+        e = expm1_taylor(x);
+    } else {
+        const double kf = rint(x / 0x1.62e42fefa39efp-1);
+        const double r = (x - kf * 0x1.62e42fee00000p-1) - kf * 0x1.a39ef35793c76p-33;
+        e = ldexp(expm1_taylor(r) + 1.0, int(kf)) - 1.0;
+    }
+    const double t = e / (e + 2.0);
+    return y < 0 ? -t : t;
+}
+// tprstb (mix_imp.f:835-856): max(tanh((-grad fac)^3), 0)
+__device__ __forceinline__ double tprstb(double grad, double fac) {
+    const double q = -grad * fac;
+    const double t = tanh_x(q * q * q);
+    return t < 0.0 ? 0.0 : t;
+}
+__device__ __forceinline__ double rho_of(const MixParams& M, double t, double s) {
+    return M.lambda * s - t - M.xes * (ALPT1 * t + ALPT2 * t * t - ALPT3 * t * t * t);
+}
+struct MixFace { double ti, si, tz, sz; };   // Ftimp, Fsimp, Ftzt, Fszt at one top face
+// fluxes through the top face kf of column (i,j) from the values below (0) and above (1)
+__device__ __forceinline__ MixFace mix_face(const Geo& g, const MixParams& M, int kf, double t0, double t1,
+                                            double s0, double s1, double iso0, double iso1) {
+    MixFace f{0.0, 0.0, 0.0, 0.0};
+    if (kf < 1) return f;                      // Ftimp(:,:,0), Ftzt(:,:,0) stay zero
+    const double w = iso1 * iso0;
+    const double den = g.dz * g.K(KT_DFZW, kf);
+    const double dt = w * (t1 - t0) / den, ds = w * (s1 - s0) / den;
+    const double dr = w * (rho_of(M, t1, s1) - rho_of(M, t0, s0)) / den;
+    if (M.eps != 0.0) {
+        const double tp = tprstb(dr, M.fac);
+        f.tz = 0.0 + tp * M.eps * dt / (dr - 1.0e-20);
+        f.sz = 0.0 + tp * M.eps * ds / (dr - 1.0e-20);
+    }
+    if (M.kvc != 0.0) {
+        const double tp = tprstb(-dr, M.fac);
+        f.ti = -(tp * M.kvc * dt);
+        f.si = -(tp * M.kvc * ds);
+    }
+    return f;
+}
+// mix(row) of the T (q = 0) or S (q = 1) row of cell (i,j,k) from the column
+// values at levels k-1, k, k+1 (the padded-field halo values at levels 0 and
+// l+1) and isoc of those levels
+__device__ __forceinline__ double mix_value(const Geo& g, const MixParams& M, int q, int k, const double* t,
+                                            const double* s, const double* iso) {
+    const MixFace lo = mix_face(g, M, k - 1, t[0], t[1], s[0], s[1], iso[0], iso[1]);
+    const MixFace up = mix_face(g, M, k, t[1], t[2], s[1], s[2], iso[1], iso[2]);
+    const double d = g.dz * g.K(KT_DFZT, k);
+    double m = 0.0;
+    if (q == 0) {
+        m = (up.tz - lo.tz) / d + m;
+        if (M.rhomix) m = ((up.ti - lo.ti) - (up.si - lo.si) * M.lambda) / (2.0 * g.dz * g.K(KT_DFZT, k)) + m;
+        else m = (up.ti - lo.ti) / d + m;
+    } else {
+        m = (up.sz - lo.sz) / d + m;
+        if (M.rhomix) m = ((up.si - lo.si) - (up.ti - lo.ti) / M.lambda) / (2.0 * g.dz * g.K(KT_DFZT, k)) + m;
+        else m = (up.si - lo.si) / d + m;
+    }
+    return m;
+}
+__device__ __forceinline__ double isoc(const Geo& g, int i, int j, int k) {
+    const int v = g.L(i, j, k);
+    return (v == OCEAN || v == PERIO) ? 1.0 : 0.0;
+}
+// the column of cell c: T, S and isoc at levels k-1, k, k+1
+__device__ __forceinline__ void mix_column(const Cell& c, double* t, double* s, double* iso) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        t[d] = c.at(3, 0, 0, d - 1);
+        s[d] = c.at(4, 0, 0, d - 1);
+        iso[d] = isoc(*c.g, c.i, c.j, c.k + d - 1);
+    }
+}
+// mix(row) of row A (TT or SS) at the current state, with vmix_fun's row flags
+template <int A>
+__device__ __forceinline__ double mix_row(const Cell& c, const MixParams& M) {
+    if (!M.on) return 0.0;
+    const int* fl = M.flags;
+    if (!((fl[0] == 1 || fl[1] == 1) && fl[4])) return 0.0;
+    if ((A == TT && fl[0] != 1) || (A == SS && fl[1] != 1)) return 0.0;
+    double t[3], s[3], iso[3];
+    mix_column(c, t, s, iso);
+    return mix_value(*c.g, M, A == TT ? 0 : 1, c.k, t, s, iso);
+}
+// vmix_jac (mix_imp.f:729-815) for row A: forward differences with step
+// 1e-8 of mix(row) in the T and S unknowns of the cells below, at and above
+// (the only ones it depends on), added to An at stencil positions 14, 5, 23.
+// The reference perturbs a whole DSM colour group at once; no other column of
+// a group touches this row, so each difference is this single-column one.
+template <int A>
+__device__ __forceinline__ void mix_jacobian(double* a, const Cell& c, const MixParams& M) {
+    if (!M.on) return;
+    const int* fl = M.flags;
+    if (!((fl[0] == 1 || fl[1] == 1) && fl[4])) return;
+    if (c.g->L(c.i, c.j, c.k) != OCEAN) return;
+    if ((A == TT && !fl[2]) || (A == SS && !fl[3])) return;
+    const bool rowon = (A == TT) ? fl[0] == 1 : fl[1] == 1;   // vmix_fun's flag for this row
+    if (!rowon) return;                                       // mixd - mix = 0 for every column
+    const Geo& g = *c.g;
+    const int q = A == TT ? 0 : 1;
+    double t[3], s[3], iso[3];
+    mix_column(c, t, s, iso);
+    const double f0 = mix_value(g, M, q, c.k, t, s, iso);
+    const double eps = 1.0e-08;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int kn = c.k + d - 1;
+        if (kn < 1 || kn > g.l || g.L(c.i, c.j, kn) != OCEAN) continue;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if ((b == 0 && !fl[2]) || (b == 1 && !fl[3])) continue;
+            double tp[3], sp[3];
+#pragma unroll
+            for (int e = 0; e < 3; ++e) { tp[e] = t[e]; sp[e] = s[e]; }
+            // und = un + d: the unknown of level kn, and every halo copy of it
+            const double pv = (b == 0 ? t[d] : s[d]) + eps;
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const int ke = c.k + e - 1;
+                const int src = ke < 1 ? 1 : (ke > g.l ? g.l : ke);
+                if (src == kn) { if (b == 0) tp[e] = pv; else sp[e] = pv; }
+            }
+            const double fj = (mix_value(g, M, q, c.k, tp, sp, iso) - f0) / eps;
+            const int kk = d == 0 ? 14 : (d == 1 ? 5 : 23);
+            if (b == 0) {
+                constexpr int e0 = idx(A, 14, TT), e1 = idx(A, 5, TT), e2 = idx(A, 23, TT);
+                const int e = kk == 14 ? e0 : (kk == 5 ? e1 : e2);
+                a[e] = a[e] + fj;
+            } else {
+                constexpr int e0 = idx(A, 14, SS), e1 = idx(A, 5, SS), e2 = idx(A, 23, SS);
+                const int e = kk == 14 ? e0 : (kk == 5 ? e1 : e2);
+                a[e] = a[e] + fj;
+            }
+        }
+    }
+}
+
+__global__ void mix_norm_part(Geo g, const double* __restrict__ x, double* __restrict__ part) {
+    const int nc = g.n * g.m * g.l;
+    double st = 0.0, ss = 0.0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const double t = x[size_t(NUN) * c + TT - 1], s = x[size_t(NUN) * c + SS - 1];
+        st += t * t;
+        ss += s * s;
+    }
+    __shared__ double red[2][256];
+    red[0][threadIdx.x] = st;
+    red[1][threadIdx.x] = ss;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + h];
+            red[1][threadIdx.x] += red[1][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = red[0][0];
+        part[2 * blockIdx.x + 1] = red[1][0];
+    }
+}
+// vmix_control (mix_imp.f:131-166): flags follow ||T||_2, ||S||_2 > 1e-12;
+// on a change the partition is rebuilt, but only when the temperature flag is
+// on (the reference tests vmix_temp twice, so a salinity-only change keeps
+// the old partition)
+__global__ void mix_control(const double* __restrict__ part, int nblocks, int* __restrict__ flags, int any_ocean) {
+    if (threadIdx.x != 0) return;
+    double st = 0.0, ss = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        st += part[2 * b];
+        ss += part[2 * b + 1];
+    }
+    const int tt = sqrt(st) > 1.0e-12 ? 1 : 0, ts = sqrt(ss) > 1.0e-12 ? 1 : 0;
+    if (flags[0] != tt || flags[1] != ts) {
+        flags[0] = tt;
+        flags[1] = ts;
+        if (tt != 0) {
+            flags[2] = tt;
+            flags[3] = ts;
+            flags[4] = any_ocean;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // boundaries (src/ocean/boundary.F90:2-393) applied to one row
 // ---------------------------------------------------------------------------
 struct Nb {
@@ -560,12 +775,13 @@ __device__ __forceinline__ void eval_row(double* a, const Cell& c, const Params&
 }
 
 template <int A>
-__device__ void jac_row(const Geo& g, const Params& P, const Pattern& pat, const double* al_tab, const Cell& c,
-                        const Nb& nb, int cell, int cls, double* val, float* val32) {
+__device__ void jac_row(const Geo& g, const Params& P, const MixParams& M, const Pattern& pat, const double* al_tab,
+                        const Cell& c, const Nb& nb, int cell, int cls, double* val, float* val32) {
     double a[rowlen(A)];
     const size_t jk = size_t(c.j - 1) + size_t(g.m) * (c.k - 1);
     const double* al_row = al_tab + (jk * 2 + (c.lm == 0.0 ? 1 : 0)) * CELL_ENTRIES;
     eval_row<A, true>(a, c, P, al_row);
+    if constexpr (A == TT || A == SS) mix_jacobian<A>(a, c, M);
     surgery<A>(a, nb);
     const int row = NUN * cell + A - 1;
     const int base = pat.row_ptr[row];
@@ -582,8 +798,9 @@ __device__ void jac_row(const Geo& g, const Params& P, const Pattern& pat, const
 }
 
 template <int A>
-__device__ void rhs_row(const Geo& g, const Params& P, const ForcingScalars& fs, const double* al_tab,
-                        const Cell& c, const Nb& nb, int cell, const double* x, const double* surf, double* F) {
+__device__ void rhs_row(const Geo& g, const Params& P, const MixParams& M, const ForcingScalars& fs,
+                        const double* al_tab, const Cell& c, const Nb& nb, int cell, const double* x,
+                        const double* surf, double* F) {
     double a[rowlen(A)];
     const size_t jk = size_t(c.j - 1) + size_t(g.m) * (c.k - 1);
     const double* al_row = al_tab + (jk * 2 + (c.lm == 0.0 ? 1 : 0)) * CELL_ENTRIES;
@@ -604,7 +821,9 @@ __device__ void rhs_row(const Geo& g, const Params& P, const ForcingScalars& fs,
         }
     });
     double frc = forcing_row<A>(g, P, fs, surf, c.i, c.j, c.k, nb);
-    double B = -acc - 0.0 + frc - 0.0 * (1 - P.par[RESC]) * 0.0;
+    double mix = 0.0;
+    if constexpr (A == TT || A == SS) mix = mix_row<A>(c, M);
+    double B = -acc - mix + frc - 0.0 * (1 - P.par[RESC]) * 0.0;
     B = B * double(1 - g.L(c.i, c.j, c.k));
     F[NUN * cell + A - 1] = -B;
 }
@@ -623,7 +842,8 @@ __device__ __forceinline__ Cell make_cell(const Geo& g, const double* pads, int 
 }
 
 // block = 6 warps; warp w evaluates row type w+1 for 32 consecutive cells
-__global__ void __launch_bounds__(192) jacobian_kernel(Geo g, Params P, Pattern pat, const double* __restrict__ al_tab,
+__global__ void __launch_bounds__(192) jacobian_kernel(Geo g, Params P, MixParams M, Pattern pat,
+                                                       const double* __restrict__ al_tab,
                                                        const double* __restrict__ pads, double* __restrict__ val,
                                                        float* __restrict__ val32) {
     const int nc = g.n * g.m * g.l;
@@ -635,17 +855,18 @@ __global__ void __launch_bounds__(192) jacobian_kernel(Geo g, Params P, Pattern 
         Nb nb = load_nb(g, c.i, c.j, c.k);
         int cls = cell_class(c.i - 1, c.j - 1, c.k - 1, g.n, g.m, g.l);
         switch (A) {
-        case UU: jac_row<UU>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
-        case VV: jac_row<VV>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
-        case WW: jac_row<WW>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
-        case PP: jac_row<PP>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
-        case TT: jac_row<TT>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
-        default: jac_row<SS>(g, P, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        case UU: jac_row<UU>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        case VV: jac_row<VV>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        case WW: jac_row<WW>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        case PP: jac_row<PP>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        case TT: jac_row<TT>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
+        default: jac_row<SS>(g, P, M, pat, al_tab, c, nb, cell, cls, val, val32); break;
         }
     }
 }
 
-__global__ void __launch_bounds__(192) rhs_kernel(Geo g, Params P, ForcingScalars fs, const double* __restrict__ al_tab,
+__global__ void __launch_bounds__(192) rhs_kernel(Geo g, Params P, MixParams M, ForcingScalars fs,
+                                                  const double* __restrict__ al_tab,
                                                   const double* __restrict__ pads, const double* __restrict__ x,
                                                   const double* __restrict__ surf, double* __restrict__ F) {
     const int nc = g.n * g.m * g.l;
@@ -656,12 +877,12 @@ __global__ void __launch_bounds__(192) rhs_kernel(Geo g, Params P, ForcingScalar
         Cell c = make_cell(g, pads, cell);
         Nb nb = load_nb(g, c.i, c.j, c.k);
         switch (A) {
-        case UU: rhs_row<UU>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
-        case VV: rhs_row<VV>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
-        case WW: rhs_row<WW>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
-        case PP: rhs_row<PP>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
-        case TT: rhs_row<TT>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
-        default: rhs_row<SS>(g, P, fs, al_tab, c, nb, cell, x, surf, F); break;
+        case UU: rhs_row<UU>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
+        case VV: rhs_row<VV>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
+        case WW: rhs_row<WW>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
+        case PP: rhs_row<PP>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
+        case TT: rhs_row<TT>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
+        default: rhs_row<SS>(g, P, M, fs, al_tab, c, nb, cell, x, surf, F); break;
         }
     }
 }
@@ -715,17 +936,21 @@ void launch_pattern(const Geo& g, const Pattern& pat, int* col_idx, cudaStream_t
     size_t work = size_t(g.n) * g.m * g.l * CELL_ENTRIES;
     pattern_kernel<<<grid_for(work, 256), 256, 0, s>>>(g, pat, col_idx); IEMIC_COUNT_LAUNCH();
 }
-void launch_jacobian(const Geo& g, const Params& p, const Pattern& pat, const double* al_tab, const double* pads,
-                     double* val, float* val32, cudaStream_t s) {
+void launch_jacobian(const Geo& g, const Params& p, const MixParams& mp, const Pattern& pat, const double* al_tab,
+                     const double* pads, double* val, float* val32, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
     size_t blocks = (nc + 31) / 32;
-    jacobian_kernel<<<int(blocks), 192, 0, s>>>(g, p, pat, al_tab, pads, val, val32); IEMIC_COUNT_LAUNCH();
+    jacobian_kernel<<<int(blocks), 192, 0, s>>>(g, p, mp, pat, al_tab, pads, val, val32); IEMIC_COUNT_LAUNCH();
 }
-void launch_rhs(const Geo& g, const Params& p, const ForcingScalars& fs, const double* al_tab, const double* pads,
-                const double* x, const double* surf, double* F, cudaStream_t s) {
+void launch_rhs(const Geo& g, const Params& p, const MixParams& mp, const ForcingScalars& fs, const double* al_tab,
+                const double* pads, const double* x, const double* surf, double* F, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
     size_t blocks = (nc + 31) / 32;
-    rhs_kernel<<<int(blocks), 192, 0, s>>>(g, p, fs, al_tab, pads, x, surf, F); IEMIC_COUNT_LAUNCH();
+    rhs_kernel<<<int(blocks), 192, 0, s>>>(g, p, mp, fs, al_tab, pads, x, surf, F); IEMIC_COUNT_LAUNCH();
+}
+void launch_mix_control(const Geo& g, const double* x, double* part, int* flags, int any_ocean, cudaStream_t s) {
+    mix_norm_part<<<152, 256, 0, s>>>(g, x, part); IEMIC_COUNT_LAUNCH();
+    mix_control<<<1, 32, 0, s>>>(part, 152, flags, any_ocean); IEMIC_COUNT_LAUNCH();
 }
 void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;

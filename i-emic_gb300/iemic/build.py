@@ -68,7 +68,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcublas"]
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr[-8000:])

@@ -13,7 +13,30 @@ OCEAN, LAND, PERIO = 0, 1, 3
 
 BASE = dict(xmin_deg=286.0, xmax_deg=350.0, ymin_deg=10.0, ymax_deg=74.0, periodic=0,
             hdim=4000.0, qz=1.0, alphaT=1.0e-4, alphaS=7.6e-4, ih=0, coriolis_on=1,
-            tres=1, sres=1, iza=2, ite=1, its=1, forcing_type=0)
+            tres=1, sres=1, iza=2, ite=1, its=1, forcing_type=0, vmix=0, rho_mixing=0, tap=1)
+
+
+def gateway_16x16x16():
+    """The reference's regression case (test/ocean/reft_ocean_params.xml,
+    driven by src/tests/reft_ocean.C): 16x16x16 cells, lon 300-340, lat 20-60,
+    periodic, depth 4000 m, uniform levels, the land mask data/mkmask/mask_gateway
+    (a basin with a periodic channel along its southern edge), vertical
+    mixing with adaptive partitioning (Mixing = 2, Taper 1, no Rho Mixing),
+    Forcing Type 2, idealized wind and T/S restoring."""
+    return dict(BASE, n=16, m=16, l=16, xmin_deg=300.0, xmax_deg=340.0, ymin_deg=20.0, ymax_deg=60.0,
+                periodic=1, hdim=4000.0, qz=1.0, iza=2, ite=1, its=1, forcing_type=2, vmix=2, rho_mixing=0,
+                tap=1)
+
+
+# "Starting Parameters" of test/ocean/reft_ocean_params.xml
+GATEWAY_STARTING_PARAMETERS = (("Combined Forcing", 0.0), ("Solar Forcing", 0.0), ("Salinity Forcing", 0.1),
+                               ("Wind Forcing", 1.0), ("Temperature Forcing", 10.0), ("SPL1", 2.0e3),
+                               ("SPL2", 0.01))
+# test/ocean/reft_continuation_params.xml (with getDefaultInitParameters for
+# the keys it leaves out)
+GATEWAY_CONTINUATION = dict(ds=2.0e-3, ds_min=1.0e-8, ds_max=1.0e-1, destination=0.02, max_steps=20,
+                            opt_newton=3.0, newton_tol=1.0e-2, destination_tol=1.0e-4, epsilon=1.0e-5,
+                            tan_scaling=1.0e-3, newton_chord=0, predictor_bound=3000.0)
 
 
 def box_16x16x4():

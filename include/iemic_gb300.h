@@ -53,6 +53,15 @@ typedef struct {
     int iza;                       /* "Wind Forcing Type": 2 idealized, else injected taux/tauy */
     int ite, its;                  /* "Levitus T/S": 1 idealized, else injected tatm/emip */
     int forcing_type;              /* "Forcing Type" */
+    int vmix;                      /* "Mixing" (vmix_GLB, src/ocean/mix_imp.f): 0 off, 1 fixed partition,
+                                      2 partition adapted to the T/S fields (Ocean::computeRHS and
+                                      computeJacobian re-evaluate it every call). The implicit vertical
+                                      mixing / convective adjustment (P_VC) and consistent vertical mixing
+                                      (ALPC < 1) terms run on the GPU; neutral physics and Gent-McWilliams
+                                      (MIXP, MKAP nonzero) are not implemented: rhs and jacobian return
+                                      IEMIC_ERR_ARG while either is nonzero with Mixing >= 1. */
+    int rho_mixing;                /* "Rho Mixing" */
+    int tap;                       /* "Taper" (tap of src/ocean/usr.F90; used by neutral physics only) */
 } iemic_config;
 
 typedef struct iemic_ocean iemic_ocean;
@@ -89,9 +98,11 @@ int iemic_jacobian_dev(iemic_ocean* h, const double* x_dev);
  * padded state fields live in one static device array of
  * IEMIC_NOALLOC_MAX_PADDED_CELLS cells per field; grids with
  * (n+2)(m+2)(l+2) above it are rejected (IEMIC_ERR_ARG). Allocates nothing.
- * The first call on a device looks the array up (cudaGetSymbolAddress) and must
- * not run during stream capture. Calls overlapping in time on one device race
- * on the shared array. Runs on the handle's stream like iemic_rhs_dev. */
+ * The first call for a device looks the array up (cudaGetSymbolAddress, with
+ * the handle's device made current) and must not run during stream capture.
+ * Runs on the handle's stream and, like iemic_rhs_dev, returns after that
+ * work has finished. Calls overlapping in time on one device (several host
+ * threads) race on the shared array. */
 #define IEMIC_NOALLOC_MAX_PADDED_CELLS 65536
 int iemic_rhs_dev_noalloc(iemic_ocean* h, const double* x_dev, double* F_dev);
 
@@ -189,7 +200,9 @@ typedef struct {
     double tol;               /* toleranceRHS_ on ||F||_2 (1e-3) */
     int backtracking_steps;   /* numBackTrackingSteps_ (10) */
     iemic_solve_opts solve;
-    int refactor_each_iter;   /* 1: new preconditioner every iteration */
+    int refactor_each_iter;   /* 1: new preconditioner every iteration; 0: the first one is kept;
+                                 2: kept while the Krylov time it costs beyond its first solve stays
+                                 below its own factorisation time, then rebuilt (see below) */
 } iemic_newton_opts;
 typedef struct {
     int iters, backtracks, linear_solves, krylov_iters, factorizations;
@@ -231,7 +244,14 @@ typedef struct {
     int give_up_at_ds_min;    /* "give up at minimum step size" */
     iemic_solve_opts solve;
     int refactor_each_newton; /* 0: preconditioner rebuilt once per step (Ocean::preProcess);
-                                 1: rebuilt after every new Jacobian */
+                                 1: rebuilt after every new Jacobian;
+                                 2: once per step, plus a rebuild on the current Jacobian as soon as
+                                    the Krylov time spent beyond the first solve's iteration count
+                                    exceeds the factorisation's own time; a solve on an older
+                                    Jacobian's factors gets only the iterations that budget still
+                                    pays for, and is repeated on fresh factors if it runs out.
+                                 Setting IEMIC_SOLVE_TRACE=1 in the environment prints one line per
+                                 solve and per step to stderr. */
 } iemic_continuation_opts;
 typedef struct {
     int steps, failed_steps, newton_iters, linear_solves, unconverged_solves, krylov_iters, factorizations;

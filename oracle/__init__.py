@@ -53,7 +53,8 @@ class Config(ctypes.Structure):
                 ("ih", ctypes.c_int), ("coriolis_on", ctypes.c_int),
                 ("tres", ctypes.c_int), ("sres", ctypes.c_int),
                 ("iza", ctypes.c_int), ("ite", ctypes.c_int), ("its", ctypes.c_int),
-                ("forcing_type", ctypes.c_int)]
+                ("forcing_type", ctypes.c_int), ("vmix", ctypes.c_int), ("rho_mixing", ctypes.c_int),
+                ("tap", ctypes.c_int)]
 
 
 class SolveOpts(ctypes.Structure):

@@ -58,6 +58,78 @@ class OracleModel:
         return self.o.get_par(idx)
 
 
+class MultifrontalModel:
+    """F and J from the C++ oracle, solves with the FP64 multifrontal LU of
+    oracle.multifrontal (all host cores; sizes where SuperLU is too slow).
+
+    policy "each": every new Jacobian is factorised and solved exactly.
+    policy "step": the reference's own preconditioner policy
+    (Ocean::preProcess, src/ocean/Ocean.C:799-808, and Ocean::solve,
+    Ocean.C:971-1147): the factorisation is rebuilt once per continuation step
+    (``pre_process``) and later Jacobians of the step are solved by GMRES
+    (restart 100) to ``tol`` preconditioned with it."""
+
+    def __init__(self, oracle, plan, policy="each", tol=1e-8):
+        self.o = oracle
+        self.plan = plan
+        self.rp, self.ci = oracle.graph()
+        self.policy = policy
+        self.tol = tol
+        self.J = None
+        self.vals = None
+        self.fact = None
+        self.fresh = False
+        self.solves = 0
+        self.factorizations = 0
+        self.krylov = 0
+
+    def rhs(self, x):
+        return self.o.rhs(x)
+
+    def jacobian(self, x):
+        from .multifrontal import Factorization   # noqa: F401
+        self.vals, _ = self.o.jacobian(x)
+        n = self.o.ndim
+        self.J = sp.csr_matrix((self.vals, self.ci, self.rp), shape=(n, n))
+        self.fresh = False
+        if self.policy == "each":
+            self.fact = None
+
+    def pre_process(self):
+        self.fact = None
+
+    def solve(self, b):
+        from .multifrontal import Factorization
+        b = np.asarray(b, dtype=np.float64)
+        self.solves += 1
+        if self.fact is None:
+            self.fact = Factorization(self.plan, self.rp, self.ci, self.vals)
+            self.factorizations += 1
+            self.fresh = True
+        if self.fresh:
+            return self.fact.solve(b)
+        n = self.o.ndim
+        M = spla.LinearOperator((n, n), matvec=self.fact.solve, dtype=np.float64)
+        count = [0]
+
+        def cb(_):
+            count[0] += 1
+
+        kw = dict(M=M, atol=0.0, restart=100, maxiter=10, callback=cb, callback_type="pr_norm")
+        try:
+            x, info = spla.gmres(self.J, b, rtol=self.tol, **kw)
+        except TypeError:   # scipy < 1.12 names the relative tolerance `tol`
+            x, info = spla.gmres(self.J, b, tol=self.tol, **kw)
+        self.krylov += count[0]
+        return x
+
+    def set_par(self, idx, v):
+        self.o.set_par(idx, v)
+
+    def get_par(self, idx):
+        return self.o.get_par(idx)
+
+
 def newton(model, x, max_iters=10, tol=1e-3, backtracking_steps=10):
     """Newton<Model>::Run: returns (x, iters, ||F||, converged)."""
     x = np.array(x, dtype=np.float64)
@@ -269,6 +341,8 @@ class Continuation:
         return 1 if res > o["newton_tol"] else 0
 
     def do_step(self):
+        if hasattr(self.M, "pre_process"):
+            self.M.pre_process()   # Ocean::preProcess: a new preconditioner once per step
         if self.euler_predictor():
             return 1
         if self.newton_corrector():

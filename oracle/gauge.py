@@ -3,7 +3,11 @@
 Restates, for CPU-side exact solves, the rule by which the GPU solver picks
 the pressure unknowns it holds at zero: per horizontally connected water
 component (columns joined by an active u/v point at any level), two adjacent
-surface pressures (a single surface pressure for a one-column component).
+surface pressures (a single surface pressure for a one-column component),
+plus one surface pressure for every further component of the diagonal
+links (i,j)-(i+1,j+1), (i+1,j)-(i,j+1) of active velocity points (a region
+joined to its basin through a single velocity point keeps a checkerboard
+mode of its own).
 Dry u/v points are those boundaries() turns into identity rows
 (src/ocean/boundary.F90): land cells, and velocities next to land to the
 north/east/north-east.
@@ -51,7 +55,35 @@ def gauge_pins(landm, n, m, l, periodic):
     def grow(i, j, k):
         return 6 * (i + n * (j + m * k)) + 3
 
+    # diagonal components: the B-grid pressure gradient at an active velocity
+    # point vanishes iff p(i,j) = p(i+1,j+1) and p(i+1,j) = p(i,j+1), so the
+    # null modes are constant on the components of these diagonal links
+    dparent = np.arange(n * m)
+
+    def dfind(a):
+        while dparent[a] != a:
+            dparent[a] = dparent[dparent[a]]
+            a = dparent[a]
+        return a
+
+    uv_point = uv_active.any(axis=0)                            # [j][i]: NE corner of cell (i, j)
+    for j in range(m):
+        for i in range(n):
+            ie = (i + 1) % n if periodic else i + 1
+            if ie >= n or j + 1 >= m or not uv_point[j, i]:
+                continue
+            dparent[dfind(i + n * j)] = dfind(ie + n * (j + 1))
+            dparent[dfind(ie + n * j)] = dfind(i + n * (j + 1))
+
     pins = []
+    pinned = set()
+
+    def pin(c):
+        r = dfind(c)
+        if r not in pinned:
+            pinned.add(r)
+            pins.append(grow(c % n, c // n, l - 1))
+
     for r in order:
         K = comps[r]
         inset = set(K)
@@ -60,16 +92,20 @@ def gauge_pins(landm, n, m, l, periodic):
             i, j = c % n, c // n
             iw = (i - 1 + n) % n if periodic else i - 1
             if iw >= 0 and (iw + n * j) in inset:
-                pins += [grow(i, j, l - 1), grow(iw, j, l - 1)]
+                pin(c)
+                pin(iw + n * j)
                 done = True
                 break
         if not done:
             for c in K:
                 i, j = c % n, c // n
                 if j > 0 and (i + n * (j - 1)) in inset:
-                    pins += [grow(i, j, l - 1), grow(i, j - 1, l - 1)]
+                    pin(c)
+                    pin(i + n * (j - 1))
                     done = True
                     break
         if not done:
-            pins.append(grow(K[0] % n, K[0] // n, l - 1))
+            pin(K[0])
+        for c in K:          # diagonal components the pair left unpinned
+            pin(c)
     return pins

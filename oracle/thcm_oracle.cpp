@@ -51,6 +51,7 @@ struct Model {
     bool periodic;
     double xmin, xmax, ymin, ymax, hdim, qz, alphaT, alphaS;
     int ih, coriolis_on, TRES, SRES, iza, ite, its, forcing_type;
+    int vmix = 0, rho_mixing = 0, tap = 1;   // "Mixing", "Rho Mixing", "Taper"
     const int coupled_T = 0, coupled_S = 0;
     // grid (src/ocean/grid.F90)
     double dx, dy, dz;
@@ -186,12 +187,14 @@ struct Model {
         par[MKAP] = 0.0;
         par[SPL1] = 2.0e+03;
         par[SPL2] = 0.01;
-        // vmix_par (src/ocean/mix_imp.f:113-128) with Mixing = 0
-        par[MIXP] = 0.0;
-        par[P_VC] = 0.0;
-        par[ALPC] = 1.0;
-        par[ENER] = 1.0e+2;
-        par[MKAP] = 0.0;
+        // vmix_par (src/ocean/mix_imp.f:113-128): only Mixing = 0 clears them
+        if (vmix == 0) {
+            par[MIXP] = 0.0;
+            par[P_VC] = 0.0;
+            par[ALPC] = 1.0;
+            par[ENER] = 1.0e+2;
+            par[MKAP] = 0.0;
+        }
     }
 
     // ---- forcing profiles: src/ocean/forcing.F90:405-449 ----
@@ -1068,16 +1071,364 @@ struct Model {
         }
     }
 
+    // =====================================================================
+    // Vertical mixing and convective adjustment (src/ocean/mix_imp.f,
+    // Mixing >= 1): vmix_init 57-111, vmix_control 131-166, vmix_part
+    // 168-228 (the partition is recorded as its row/column flags), vmix_fun
+    // 231-562 with dCdxt/dCdyt/dCdzt/drhodC/tprslp 564-727, vmix_jac
+    // 729-815, isoc 817-833, tprstb 835-856, vmix_el_1/vmix_el_2 858-1050.
+    // =====================================================================
+    int vmix_flag = 0, vmix_temp = 0, vmix_salt = 0, vmix_fix = 1;
+    int part_temp = 0, part_salt = 0;   // row/column sets of the current partition
+    long vmix_dim = 0;                  // NPAIRS of the current partition
+
+    void vmix_init() {
+        if (vmix == 0) { vmix_flag = 0; vmix_fix = 1; }
+        else if (vmix == 1) { vmix_flag = 1; vmix_fix = 1; }
+        else if (vmix == 2) { vmix_flag = 2; vmix_fix = 0; }
+        else vmix_flag = -1;
+        if (vmix_flag == 0) { vmix_temp = 0; vmix_salt = 0; }
+        else if (vmix_flag == 1) { vmix_temp = 1; vmix_salt = 1; vmix_part(); }
+        else if (vmix_flag == 2) { vmix_temp = 0; vmix_salt = 0; }
+    }
+    static double l2nrm_stride(const double* f, int count, int stride) {   // matetc.F90:22-36
+        double nrm = 0.0;
+        for (int i = 0; i < count; ++i) nrm = f[size_t(i) * stride] * f[size_t(i) * stride] + nrm;
+        return std::sqrt(nrm);
+    }
+    void vmix_control(const double* un) {
+        int test_temp = l2nrm_stride(un + TT - 1, n * m * l, NUN) > 1.0e-12 ? 1 : 0;
+        int test_salt = l2nrm_stride(un + SS - 1, n * m * l, NUN) > 1.0e-12 ? 1 : 0;
+        if (vmix_temp != test_temp || vmix_salt != test_salt) {
+            vmix_temp = test_temp;
+            vmix_salt = test_salt;
+            if (vmix_temp != 0 && vmix_temp != 0) vmix_part();   // (sic) the reference tests vmix_temp twice
+        }
+        vmix_fix = 1;
+    }
+    // vmix_el_1 (flag 1: T and S rows, T and S columns) / vmix_el_2 (flag 2:
+    // rows and columns of the fields switched on). Only the flags and the
+    // count matter here: the pairs themselves are enumerated again in vmix_jac.
+    void vmix_part() {
+        part_temp = vmix_flag == 1 ? 1 : vmix_temp;
+        part_salt = vmix_flag == 1 ? 1 : vmix_salt;
+        long p = 0;
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            if (LM(i, j, k) != OCEAN) continue;
+            for (int h = 0; h < 27; ++h) {
+                const int kind = LM(i + ST[h][0], j + ST[h][1], k + ST[h][2]);
+                if (kind == OCEAN || kind == PERIO) p += long(part_temp + part_salt) * (part_temp + part_salt);
+            }
+        }
+        vmix_dim = p;
+    }
+    // st(27,:) of vmix_el_1 / vmix_el_2: (di, dj, dk) per stencil point
+    static constexpr int ST[27][3] = {
+        {-1, -1, -1}, {-1, 0, -1}, {-1, 1, -1}, {0, -1, -1}, {0, 0, -1}, {0, 1, -1}, {1, -1, -1}, {1, 0, -1},
+        {1, 1, -1},   {-1, -1, 0}, {-1, 0, 0},  {-1, 1, 0},  {0, -1, 0}, {0, 0, 0},  {0, 1, 0},  {1, -1, 0},
+        {1, 0, 0},    {1, 1, 0},   {-1, -1, 1}, {-1, 0, 1},  {-1, 1, 1}, {0, -1, 1}, {0, 0, 1},  {0, 1, 1},
+        {1, -1, 1},   {1, 0, 1},   {1, 1, 1}};
+
+    double isoc(int i, int j, int k) { return (LM(i, j, k) == OCEAN || LM(i, j, k) == PERIO) ? 1.0 : 0.0; }
+
+    // tanh(y) by one explicit algorithm, the same operation sequence as the
+    // GPU kernels': the reference calls the platform libm, whose last bit is
+    // implementation-defined (glibc and CUDA differ). |y| < 2^-27 returns y,
+    // |y| > 22 returns +-1 (tanh is 1 to the last bit there); otherwise
+    // tanh(y) = e / (e + 2) with e = expm1(2|y|): a Taylor series of degree 13
+    // below ln2/2, else Cody-Waite reduction x = k ln2 + r (ln2 split into a
+    // 32-bit head and a tail) and 2^k (1 + expm1(r)) - 1.
+    static double expm1_taylor(double r) {
+        static const double c[13] = {0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29, 0x1.ae64567f544e4p-26,
+                                     0x1.27e4fb7789f5cp-22, 0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16,
+                                     0x1.a01a01a01a01ap-13, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7,
+                                     0x1.5555555555555p-5,  0x1.5555555555555p-3,  0x1.0p-1,
+                                     0x1.0p+0};   // 1/13!, 1/12!, ..., 1/1!
+        double p = c[0];
+        for (int q = 1; q < 13; ++q) p = p * r + c[q];
+        return p * r;
+    }
+    static double tanh_x(double y) {
+        const double a = std::fabs(y);
+        if (!(a >= 0x1p-27)) return y;
+        if (a > 22.0) return y > 0 ? 1.0 : -1.0;
+        const double x = 2.0 * a;
+        double e;
+        if (x <= 0x1.62e42fefa39efp-2) {
+            e = expm1_taylor(x);
+        } else {
+            const double kf = std::nearbyint(x / 0x1.62e42fefa39efp-1);
+            const double r = (x - kf * 0x1.62e42fee00000p-1) - kf * 0x1.a39ef35793c76p-33;
+            e = std::ldexp(expm1_taylor(r) + 1.0, int(kf)) - 1.0;
+        }
+        const double t = e / (e + 2.0);
+        return y < 0 ? -t : t;
+    }
+    double tprstb(double grad, double spl) const {   // mix_imp.f:835-856
+        const double fac = alphaT * spl;
+        const double q = -grad * fac;
+        return std::max(tanh_x(q * q * q), 0.0);
+    }
+    void tprslp(double drdh, double drdz, double spl, double& slp, double& tpr) const {   // mix_imp.f:660-727
+        const double width = 1.0, epsln = 1.0e-20;
+        if (drdz == 0.0) drdz = epsln;
+        slp = -drdh / drdz;
+        const double absslp = std::sqrt(slp * slp);
+        const double delta = (r0dim / hdim) * spl;
+        const double sd = width * delta;
+        if (tap == 1) {
+            if (absslp > delta) { const double q = delta / absslp; tpr = q * q; }
+            else tpr = 1.0;
+        } else if (tap == 2) {
+            tpr = 0.5 * (1.0 - tanh_x((absslp - delta) / sd));
+        } else if (tap == 3) {
+            if (absslp < delta - sd && drdz < 0.0) tpr = 1.0;
+            else if (absslp >= delta - sd && absslp < delta && drdz < 0.0) {
+                const double dum = (absslp - (delta - sd)) / sd;
+                tpr = 1.0 - 3.0 * (dum * dum) + 2.0 * (dum * dum * dum);
+            } else tpr = 0.0;
+        } else {
+            tpr = 1.0;
+        }
+    }
+
+    // vmix_fun (mix_imp.f:231-562): divergence of the diffusive T/S fluxes
+    void vmix_fun(const double* un, double* mix) {
+        usol(un);
+        Arr3 T = t, S = s;
+        const double xes = par[NLES], lambda = par[LAMB];
+        const double piso = par[MIXP] * par[PE_H], pgm = par[MKAP] * par[PE_H];
+        const double eps = (1.0 - par[ALPC]) * par[ENER] * par[PE_V];
+        const double kvc = par[P_VC], sp1 = par[SPL1], sp2 = par[SPL2];
+        const double epsln = 1.0e-20;
+        auto dCdxt = [&](Arr3& C) {
+            Arr3 d(0, n, 0, m + 1, 0, l + 1);
+            for (int k = 0; k <= l + 1; ++k) for (int j = 0; j <= m + 1; ++j) for (int i = 0; i <= n; ++i)
+                d(i, j, k) = isoc(i + 1, j, k) * isoc(i, j, k) * (C(i + 1, j, k) - C(i, j, k)) / (dx * std::cos(Y(j)));
+            return d;
+        };
+        auto dCdyt = [&](Arr3& C) {
+            Arr3 d(0, n + 1, 0, m, 0, l + 1);
+            for (int k = 0; k <= l + 1; ++k) for (int j = 0; j <= m; ++j) for (int i = 0; i <= n + 1; ++i)
+                d(i, j, k) = isoc(i, j + 1, k) * isoc(i, j, k) * (C(i, j + 1, k) - C(i, j, k)) / dy;
+            return d;
+        };
+        auto dCdzt = [&](Arr3& C) {
+            Arr3 d(0, n + 1, 0, m + 1, 0, l);
+            for (int k = 0; k <= l; ++k) for (int j = 0; j <= m + 1; ++j) for (int i = 0; i <= n + 1; ++i)
+                d(i, j, k) = isoc(i, j, k + 1) * isoc(i, j, k) * (C(i, j, k + 1) - C(i, j, k)) / (dz * DFZW(k));
+            return d;
+        };
+        Arr3 dtdxe = dCdxt(T), dsdxe = dCdxt(S), dtdyn = dCdyt(T), dsdyn = dCdyt(S);
+        Arr3 dtdzt = dCdzt(T), dsdzt = dCdzt(S);
+        Arr3 rho(0, n + 1, 0, m + 1, 0, l + 1), drhodt(0, n + 1, 0, m + 1, 0, l + 1), drhods(0, n + 1, 0, m + 1, 0, l + 1);
+        for (size_t q = 0; q < rho.d.size(); ++q) {
+            const double tt = T.d[q], ss = S.d[q];
+            rho.d[q] = lambda * ss - tt - xes * (alpt1 * tt + alpt2 * tt * tt - alpt3 * tt * tt * tt);
+            drhodt.d[q] = -1.0 - xes * (alpt1 + 2.0 * alpt2 * tt - 3.0 * alpt3 * (tt * tt));
+            drhods.d[q] = lambda;
+        }
+        Arr3 drhodzt = dCdzt(rho);
+        Arr3 Ftxe(0, n, 1, m, 1, l), Fsxe(0, n, 1, m, 1, l), Ftyn(1, n, 0, m, 1, l), Fsyn(1, n, 0, m, 1, l);
+        Arr3 Ftzt(1, n, 1, m, 0, l), Fszt(1, n, 1, m, 0, l), Ftimp(1, n, 1, m, 0, l), Fsimp(1, n, 1, m, 0, l);
+        const bool np_gm = piso != 0.0 || pgm != 0.0;
+        auto east_face = [&](int i, int j, int k) {
+            double dumt = 0.0, dums = 0.0;
+            for (int kr = 0; kr <= 1; ++kr) for (int ip = 0; ip <= 1; ++ip) {
+                const double drdh = drhodt(i + ip, j, k) * dtdxe(i, j, k) + drhods(i + ip, j, k) * dsdxe(i, j, k);
+                const double drdz = drhodt(i + ip, j, k) * dtdzt(i + ip, j, k - 1 + kr) +
+                                    drhods(i + ip, j, k) * dsdzt(i + ip, j, k - 1 + kr);
+                double slp, tpr;
+                tprslp(drdh, drdz, sp2, slp, tpr);
+                dumt = dumt + DFZW(k - 1 + kr) * (tpr * (piso)*dtdxe(i, j, k) + tpr * (piso - pgm) * slp * dtdzt(i + ip, j, k - 1 + kr));
+                dums = dums + DFZW(k - 1 + kr) * (tpr * (piso)*dsdxe(i, j, k) + tpr * (piso - pgm) * slp * dsdzt(i + ip, j, k - 1 + kr));
+            }
+            Ftxe(i, j, k) = Ftxe(i, j, k) - dumt / (4 * DFZT(k));
+            Fsxe(i, j, k) = Fsxe(i, j, k) - dums / (4 * DFZT(k));
+        };
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) {
+            if (np_gm) east_face(0, j, k);
+            for (int i = 1; i <= n; ++i) {
+                if (np_gm) {
+                    east_face(i, j, k);
+                    double dumt = 0.0, dums = 0.0;   // north face
+                    for (int kr = 0; kr <= 1; ++kr) for (int jq = 0; jq <= 1; ++jq) {
+                        const double drdh = drhodt(i, j + jq, k) * dtdyn(i, j, k) + drhods(i, j + jq, k) * dsdyn(i, j, k);
+                        const double drdz = drhodt(i, j + jq, k) * dtdzt(i, j + jq, k - 1 + kr) +
+                                            drhods(i, j + jq, k) * dsdzt(i, j + jq, k - 1 + kr);
+                        double slp, tpr;
+                        tprslp(drdh, drdz, sp2, slp, tpr);
+                        dumt = dumt + DFZW(k - 1 + kr) * std::cos(Y(j + jq)) *
+                                          (tpr * (piso)*dtdyn(i, j, k) + tpr * (piso - pgm) * slp * dtdzt(i, j + jq, k - 1 + kr));
+                        dums = dums + DFZW(k - 1 + kr) * std::cos(Y(j + jq)) *
+                                          (tpr * (piso)*dsdyn(i, j, k) + tpr * (piso - pgm) * slp * dsdzt(i, j + jq, k - 1 + kr));
+                    }
+                    Ftyn(i, j, k) = Ftyn(i, j, k) - dumt / (4 * DFZT(k) * std::cos(YV(j)));
+                    Fsyn(i, j, k) = Fsyn(i, j, k) - dums / (4 * DFZT(k) * std::cos(YV(j)));
+                    dumt = 0.0; dums = 0.0;   // top face, zonal variations
+                    for (int ip = 0; ip <= 1; ++ip) for (int kr = 0; kr <= 1; ++kr) {
+                        const double drdh = drhodt(i, j, k + kr) * dtdxe(i - 1 + ip, j, k + kr) +
+                                            drhods(i, j, k + kr) * dsdxe(i - 1 + ip, j, k + kr);
+                        const double drdz = drhodt(i, j, k + kr) * dtdzt(i, j, k) + drhods(i, j, k + kr) * dsdzt(i, j, k);
+                        double slp, tpr;
+                        tprslp(drdh, drdz, sp2, slp, tpr);
+                        dumt = dumt + (tpr * (piso)*slp * slp * dtdzt(i, j, k) + tpr * (piso + pgm) * slp * dtdxe(i - 1 + ip, j, k + kr));
+                        dums = dums + (tpr * (piso)*slp * slp * dsdzt(i, j, k) + tpr * (piso + pgm) * slp * dsdxe(i - 1 + ip, j, k + kr));
+                    }
+                    Ftzt(i, j, k) = Ftzt(i, j, k) - dumt / 4;
+                    Fszt(i, j, k) = Fszt(i, j, k) - dums / 4;
+                    dumt = 0.0; dums = 0.0;   // top face, meridional variations
+                    for (int jq = 0; jq <= 1; ++jq) for (int kr = 0; kr <= 1; ++kr) {
+                        const double drdh = drhodt(i, j, k + kr) * dtdyn(i, j - 1 + jq, k + kr) +
+                                            drhods(i, j, k + kr) * dsdyn(i, j - 1 + jq, k + kr);
+                        const double drdz = drhodt(i, j, k + kr) * dtdzt(i, j, k) + drhods(i, j, k + kr) * dsdzt(i, j, k);
+                        double slp, tpr;
+                        tprslp(drdh, drdz, sp2, slp, tpr);
+                        dumt = dumt + (tpr * (piso)*slp * slp * dtdzt(i, j, k) + tpr * (piso + pgm) * slp * dtdyn(i, j - 1 + jq, k + kr));
+                        dums = dums + (tpr * (piso)*slp * slp * dsdzt(i, j, k) + tpr * (piso + pgm) * slp * dsdyn(i, j - 1 + jq, k + kr));
+                    }
+                    Ftzt(i, j, k) = Ftzt(i, j, k) - dumt / 4;
+                    Fszt(i, j, k) = Fszt(i, j, k) - dums / 4;
+                }
+                if (eps != 0.0) {   // consistent vertical mixing
+                    const double d = drhodzt(i, j, k);
+                    Ftzt(i, j, k) = Ftzt(i, j, k) + tprstb(d, sp1) * eps * dtdzt(i, j, k) / (d - epsln);
+                    Fszt(i, j, k) = Fszt(i, j, k) + tprstb(d, sp1) * eps * dsdzt(i, j, k) / (d - epsln);
+                }
+                if (kvc != 0.0) {   // implicit vertical mixing (convective adjustment)
+                    Ftimp(i, j, k) = -(tprstb(-drhodzt(i, j, k), sp1) * kvc * dtdzt(i, j, k));
+                    Fsimp(i, j, k) = -(tprstb(-drhodzt(i, j, k), sp1) * kvc * dsdzt(i, j, k));
+                }
+            }
+        }
+        const bool rhomix = rho_mixing != 0 && xes == 0.0;
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            const double cy = std::cos(Y(j));
+            int row = find_row2(i, j, k, TT) - 1;
+            mix[row] = 0.0;
+            if (vmix_temp == 1) {
+                mix[row] = (Ftxe(i, j, k) - Ftxe(i - 1, j, k)) / (dx * cy) + mix[row];
+                mix[row] = (Ftyn(i, j, k) * std::cos(YV(j)) - Ftyn(i, j - 1, k) * std::cos(YV(j - 1))) / (dy * cy) + mix[row];
+                mix[row] = (Ftzt(i, j, k) - Ftzt(i, j, k - 1)) / (dz * DFZT(k)) + mix[row];
+                if (rhomix)
+                    mix[row] = ((Ftimp(i, j, k) - Ftimp(i, j, k - 1)) - (Fsimp(i, j, k) - Fsimp(i, j, k - 1)) * lambda) /
+                                   (2.0 * dz * DFZT(k)) + mix[row];
+                else
+                    mix[row] = (Ftimp(i, j, k) - Ftimp(i, j, k - 1)) / (dz * DFZT(k)) + mix[row];
+            }
+            row = find_row2(i, j, k, SS) - 1;
+            mix[row] = 0.0;
+            if (vmix_salt == 1) {
+                mix[row] = (Fsxe(i, j, k) - Fsxe(i - 1, j, k)) / (dx * cy) + mix[row];
+                mix[row] = (Fsyn(i, j, k) * std::cos(YV(j)) - Fsyn(i, j - 1, k) * std::cos(YV(j - 1))) / (dy * cy) + mix[row];
+                mix[row] = (Fszt(i, j, k) - Fszt(i, j, k - 1)) / (dz * DFZT(k)) + mix[row];
+                if (rhomix)
+                    mix[row] = ((Fsimp(i, j, k) - Fsimp(i, j, k - 1)) - (Ftimp(i, j, k) - Ftimp(i, j, k - 1)) / lambda) /
+                                   (2.0 * dz * DFZT(k)) + mix[row];
+                else
+                    mix[row] = (Fsimp(i, j, k) - Fsimp(i, j, k - 1)) / (dz * DFZT(k)) + mix[row];
+            }
+        }
+    }
+
+    // vmix_jac (mix_imp.f:729-815): forward differences (eps = 1e-8) over a
+    // column partition, added into An at the stencil position of each pair.
+    // The partition here colours columns by (i mod 3 or i, j mod 3, k mod 3,
+    // field); any partition in which no two columns of a group share a row
+    // of the 27-point pattern (such as DSM's) yields the same values: each
+    // row's difference then sees exactly one perturbed column of its group.
+    void vmix_jac(const double* un) {
+        const double eps = 1.0e-08;
+        std::vector<double> mix(ndim, 0.0), mixd(ndim, 0.0), und(ndim);
+        vmix_fun(un, mix.data());
+        const bool wrap3 = periodic && (n % 3 != 0);
+        auto group_of = [&](int i, int j, int k, int XX) {
+            const int ci = wrap3 ? i : (i % 3);
+            return ((ci * 3 + j % 3) * 3 + k % 3) * 2 + (XX == SS ? 1 : 0);
+        };
+        const int ngroups = (wrap3 ? n + 1 : 3) * 9 * 2;
+        // fjac per (row cell, h, row field, column field)
+        std::vector<double> fj(size_t(n) * m * l * 27 * 4, 0.0);
+        auto fjx = [&](int i, int j, int k, int h, int a, int b) -> double& {
+            return fj[(((cell(i, j, k) * 27 + h) * 2 + a) * 2 + b)];
+        };
+        for (int g = 0; g < ngroups; ++g) {
+            bool any = false;
+            for (int r = 0; r < ndim; ++r) und[r] = un[r];
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+                for (int XX : {TT, SS}) {
+                    if ((XX == TT && !part_temp) || (XX == SS && !part_salt)) continue;
+                    if (group_of(i, j, k, XX) != g) continue;
+                    const int c = find_row2(i, j, k, XX) - 1;
+                    und[c] = un[c] + eps;
+                    any = true;
+                }
+            if (!any) continue;
+            vmix_fun(und.data(), mixd.data());
+            for (int r = 0; r < ndim; ++r) mixd[r] = mixd[r] - mix[r];
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+                if (LM(i, j, k) != OCEAN) continue;
+                for (int a = 0; a < 2; ++a) {
+                    if ((a == 0 && !part_temp) || (a == 1 && !part_salt)) continue;
+                    const int row = find_row2(i, j, k, a == 0 ? TT : SS) - 1;
+                    for (int h = 0; h < 27; ++h) {
+                        const int I = i + ST[h][0], J = j + ST[h][1], K = k + ST[h][2];
+                        const int kind = LM(I, J, K);
+                        if (kind != OCEAN && kind != PERIO) continue;
+                        const int ci = kind == PERIO ? i - ST[h][0] * (n - 1) : I;
+                        for (int b = 0; b < 2; ++b) {
+                            if ((b == 0 && !part_temp) || (b == 1 && !part_salt)) continue;
+                            if (group_of(ci, J, K, b == 0 ? TT : SS) != g) continue;
+                            fjx(i, j, k, h, a, b) = mixd[row] / eps;
+                        }
+                    }
+                }
+            }
+        }
+        // scatter into An(s, ie, je, ix, iy, iz)
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i) {
+            if (LM(i, j, k) != OCEAN) continue;
+            for (int h = 0; h < 27; ++h) {
+                const int I = i + ST[h][0], J = j + ST[h][1], K = k + ST[h][2];
+                const int kind = LM(I, J, K);
+                if (kind != OCEAN && kind != PERIO) continue;
+                const int jx = kind == PERIO ? i - ST[h][0] * (n - 1) : I;
+                int sidx = 0;
+                if (K - k == -1) sidx += 9;
+                if (K - k == 1) sidx += 18;
+                if (jx - i == 0) sidx += 3;
+                if (jx - i == 1) sidx += 6;
+                if (jx - i == 1 - n) sidx += 6;
+                if (J - j == -1) sidx += 1;
+                if (J - j == 0) sidx += 2;
+                if (J - j == 1) sidx += 3;
+                for (int a = 0; a < 2; ++a) {
+                    if ((a == 0 && !part_temp) || (a == 1 && !part_salt)) continue;
+                    for (int b = 0; b < 2; ++b) {
+                        if ((b == 0 && !part_temp) || (b == 1 && !part_salt)) continue;
+                        double& an = AN(sidx, a == 0 ? TT : SS, b == 0 ? TT : SS, i, j, k);
+                        an = an + fjx(i, j, k, h, a, b);
+                    }
+                }
+            }
+        }
+    }
+
     // ---- rhs: src/ocean/usrc.F90:523-603, sign flip of THCM.C:1008-1011 ----
     void rhs(const double* un, double* F) {
+        std::vector<double> mix(ndim, 0.0);
         An = Al;
         nlin_rhs(un);
         boundaries();
         fillcolA();
         std::vector<double> Au(ndim);
         matAvec(un, Au.data());
+        if (vmix_flag >= 1) {   // usrc.F90:551-569
+            if (vmix_fix == 0 && vmix_flag >= 2) vmix_control(un);
+            if ((vmix_temp == 1 || vmix_salt == 1) && vmix_dim > 0) vmix_fun(un, mix.data());
+        }
         for (int r = 0; r < ndim; ++r) {
-            double B = -Au[r] - 0.0 + Frc[r] - 0.0 * (1 - par[RESC]) * 0.0;
+            double B = -Au[r] - mix[r] + Frc[r] - 0.0 * (1 - par[RESC]) * 0.0;
             F[r] = B;
         }
         for (int i = 1; i <= n; ++i) for (int j = 1; j <= m; ++j) for (int k = 1; k <= l; ++k)
@@ -1098,6 +1449,10 @@ struct Model {
         An = Al;
         fillcolB();
         nlin_jac(un);
+        if (vmix_flag >= 1) {   // usrc.F90:488-508
+            if (vmix_fix == 0 && vmix_flag >= 2) vmix_control(un);
+            if ((vmix_temp == 1 || vmix_salt == 1) && vmix_dim > 0) vmix_jac(un);
+        }
         boundaries();
         fillcolA();
     }
@@ -1208,6 +1563,7 @@ struct Model {
         hdim = c.hdim; qz = c.qz; alphaT = c.alphaT; alphaS = c.alphaS;
         ih = c.ih; coriolis_on = c.coriolis_on; TRES = c.tres; SRES = c.sres;
         iza = c.iza; ite = c.ite; its = c.its; forcing_type = c.forcing_type;
+        vmix = c.vmix; rho_mixing = c.rho_mixing; tap = c.tap;
         landm.assign(size_t(n + 2) * (m + 2) * (l + 2), OCEAN);
         if (lm) {
             for (size_t q = 0; q < landm.size(); ++q) landm[q] = lm[q];
@@ -1235,6 +1591,7 @@ struct Model {
         stpnt();
         forcing();
         lin();
+        vmix_init();   // usrc.F90:133
         build_graph();
     }
 };
@@ -1294,6 +1651,7 @@ void oracle_get_grid(void* h, double* x, double* y, double* xu, double* yv, doub
 }
 void oracle_rhs(void* h, const double* x, double* F) {
     Model* M = static_cast<Model*>(h);
+    if (M->vmix == 2) M->vmix_fix = 0;   // Ocean::computeRHS -> THCM::fixMixing(0) (Ocean.C:1281; THCM.C:2640-2647)
     // forcing() is re-run because boundaries() zeroes Frc entries in place,
     // exactly like the reference, where Frc persists across calls.
     M->rhs(x, F);
@@ -1314,6 +1672,7 @@ void oracle_graph(void* h, int* row_ptr, int* col_idx) {
 }
 int oracle_jacobian(void* h, const double* x, double* values) {
     Model* M = static_cast<Model*>(h);
+    if (M->vmix == 2) M->vmix_fix = 0;   // Ocean::computeJacobian -> THCM::fixMixing(0) (Ocean.C:1302)
     M->matrix(x);
     return M->scatter(values);
 }

@@ -8,11 +8,15 @@
 // it; the GPU product never links or calls it.
 //
 // Parity status: the reference cannot be compiled here (no Fortran compiler,
-// no Trilinos/MPI), and it ships no golden values for J or F entries of a
-// Mixing=0 ocean. The restatement is pinned to the reference's own
-// known-answer tests instead (src/tests/test_ocean.C: F(0)=0 at zero forcing,
-// exact mass-matrix values, salt-conservation column integrals; and
-// src/tests/TestDefinitions.H: analytic vs finite-difference Jacobian).
+// no Trilinos/MPI), and it ships no golden values for J or F entries. The
+// restatement is pinned to the reference's own known-answer tests
+// (src/tests/test_ocean.C: F(0)=0 at zero forcing, exact mass-matrix values,
+// salt-conservation column integrals; src/tests/TestDefinitions.H: analytic
+// vs finite-difference Jacobian) and to the reference-produced state of
+// test/ocean/ocean_reference.h5: the steady state the reference's
+// src/tests/reft_ocean.C reaches by continuation on the 16x16x16 gateway mask
+// with vertical mixing (Mixing = 2), checked through the u, v, T, S norms
+// that test compares.
 #pragma once
 #include <cstdint>
 
@@ -33,6 +37,9 @@ typedef struct {
     int iza;                  // "Wind Forcing Type" (2 = idealized Bryan profile, else injected)
     int ite, its;             // "Levitus T/S" (1 = idealized profile, else injected)
     int forcing_type;         // "Forcing Type"
+    int vmix;                 // "Mixing" (vmix_GLB): 0 off, 1 fixed partition, 2 adaptive
+    int rho_mixing;           // "Rho Mixing"
+    int tap;                  // "Taper" (tap in usr.F90)
 } iemic_oracle_config;
 
 void* oracle_create(const iemic_oracle_config* cfg, const int* landm);

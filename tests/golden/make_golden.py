@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures of tests/golden/ (run from the repository root).
 
 1. mask_global_96x38x12.npy: the reference's real-continent land mask
-   data/mkmask/mask_global_96x38x12 (read only when the reference checkout is
-   available), converted with the reader rules of readmask
+   data/mkmask/mask_global_96x38x12 (read only when ``--reference PATH`` names
+   a checkout of the reference), converted with the reader rules of readmask
    (src/ocean/topo.F90:41-60): per level k = 0..l+1 a header line, then rows
    j = m+1 down to 0 of n+2 digits (i = 0..n+1). Stored as int8 in the
    (l+2, m+2, n+2) layout of the C ABI (i fastest).
@@ -46,9 +46,14 @@ def oracle_summary(o, x):
 
 
 def main():
+    import argparse
     from helpers import box_case, global_case, make_oracle, seeded_state
-    ref_mask = "/root/reference/data/mkmask/mask_global_96x38x12"
-    if os.path.exists(ref_mask):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="root of the reference checkout (for the real-continent mask)")
+    args = ap.parse_args()
+    ref_mask = None if args.reference is None else os.path.join(args.reference, "data", "mkmask",
+                                                                 "mask_global_96x38x12")
+    if ref_mask is not None and os.path.exists(ref_mask):
         np.save(os.path.join(HERE, "mask_global_96x38x12.npy"), read_mask(ref_mask, 96, 38, 12))
     for name, case, seed in (("box_seed0", box_case, 0), ("glob24_seed1", global_case, 1)):
         cfg, lm, frc = case()

@@ -1,11 +1,29 @@
 """Shared builders for the test suite: the same seeded workloads on the
 oracle (CPU, checker only) and on the GPU engine."""
+import os
+
 import numpy as np
 
 from iemic import workloads as W
 
 ORACLE_PAR = {"Combined Forcing": "COMB", "Temperature Forcing": "TEMP",
-              "Salinity Forcing": "SALT", "Wind Forcing": "WIND"}
+              "Salinity Forcing": "SALT", "Wind Forcing": "WIND", "Solar Forcing": "SUNP",
+              "SPL1": "SPL1", "SPL2": "SPL2"}
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def gateway_case(vmix=2):
+    """The reference's regression case (reft_ocean) with the land mask THCM
+    used, as stored in test/ocean/ocean_reference.h5."""
+    g = np.load(os.path.join(GOLDEN, "reft_ocean_reference.npz"))
+    cfg = dict(W.gateway_16x16x16(), vmix=vmix)
+    return cfg, g["landm"].astype(np.int32), None
+
+
+def gateway_golden():
+    g = np.load(os.path.join(GOLDEN, "reft_ocean_reference.npz"))
+    pars = dict(zip([str(s) for s in g["par_names"]], g["par_values"]))
+    return g["state"], pars
 
 
 def box_case():

@@ -2,16 +2,19 @@
 it must pass alone and after every other test in the process).
 
 Two calls in a row on the same handle, each compared bit for bit with the
-handle-scratch entry point, on the 16x16x4 box and a 24x12x6 periodic
-global ocean; a grid whose padded fields exceed the static scratch is
-rejected without touching the output.
+handle-scratch entry point, on the 16x16x4 box, a 24x12x6 periodic global
+ocean and the 16x16x16 gateway basin with vertical mixing (whose partition
+control also keeps its partial sums in the static array); calls on two
+handles back to back, read on another stream right after each returns; a
+grid whose padded fields exceed the static scratch is rejected without
+touching the output.
 """
 import ctypes
 
 import numpy as np
 import pytest
 
-from helpers import box_case, global_case, make_gpu, seeded_state
+from helpers import box_case, gateway_case, global_case, make_gpu, seeded_state
 
 pytestmark = pytest.mark.gpu
 
@@ -25,11 +28,16 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-@pytest.mark.parametrize("case", [box_case, global_case])
+def _gateway():
+    return gateway_case(2)
+
+
+@pytest.mark.parametrize("case", [box_case, global_case, _gateway])
 def test_noalloc_rhs_matches_rhs_dev_twice(case):
     import torch
+    from iemic import workloads as W
     cfg, lm, frc = case()
-    g = make_gpu(cfg, lm, frc)
+    g = make_gpu(cfg, lm, frc, W.GATEWAY_STARTING_PARAMETERS if cfg.get("vmix") else W.STARTING_PARAMETERS)
     L = g.L
     for seed in (0, 1):   # two calls in a row, different states
         x = _dev(seeded_state(cfg, seed, uvw=0.01))
@@ -41,6 +49,30 @@ def test_noalloc_rhs_matches_rhs_dev_twice(case):
         a, b = F_ref.cpu().numpy(), F_na.cpu().numpy()
         assert np.array_equal(a.view(np.int64), b.view(np.int64))
         assert np.linalg.norm(a) > 0
+
+
+def test_noalloc_two_handles_back_to_back():
+    """Each call has finished when it returns: the result is read at once on
+    torch's stream (not the handle's), and the next call, on another handle,
+    reuses the shared array."""
+    import torch
+    cases = [box_case(), global_case()]
+    hs = [make_gpu(*c) for c in cases]
+    xs = [_dev(seeded_state(c[0], 4 + q, uvw=0.01)) for q, c in enumerate(cases)]
+    refs = []
+    for g, x in zip(hs, xs):
+        F = torch.zeros(g.ndim, dtype=torch.float64, device="cuda")
+        assert g.L.iemic_rhs_dev(g.handle, _ptr(x), _ptr(F)) == 0
+        refs.append(F.cpu().numpy())
+    for _ in range(2):
+        got = []
+        for g, x in zip(hs, xs):
+            F = torch.full((g.ndim,), np.nan, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            assert g.L.iemic_rhs_dev_noalloc(g.handle, _ptr(x), _ptr(F)) == 0
+            got.append(F.clone())          # ordered on torch's stream, after the call returned
+        for r, F in zip(refs, got):
+            assert np.array_equal(r.view(np.int64), F.cpu().numpy().view(np.int64))
 
 
 def test_noalloc_rejects_grids_over_the_scratch():
