@@ -23,6 +23,7 @@
 // SpMV: rows hold 7..24 entries, so four lanes share a row and reduce with
 // warp shuffles; a warp covers eight consecutive rows (contiguous loads of
 // col_idx/values). The state vectors stay resident in the 126 MB L2.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -150,6 +151,149 @@ __global__ void add_to(int n, const T* __restrict__ d, T* __restrict__ x) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) x[r] += d[r];
 }
 
+// ---- device-driven Arnoldi cycle ------------------------------------------
+// Control block: j = Hessenberg columns done in this cycle, it = inner
+// iterations of the solve, stop = 0 running, 1 converged, 2 lucky breakdown
+// (the new basis vector vanished), 3 cycle full or iteration cap, 4 a
+// non-finite value.
+}  // namespace
+struct KryCtl {
+    int j, it, maxit, m, stop, pad;
+    double beta0, tol, relres, hn2, inv_hn;
+};
+namespace {
+__global__ void k_cycle_init(KryCtl* __restrict__ ctl, double* __restrict__ g, int m, double beta, double beta0,
+                             double tol, int it, int maxit) {
+    for (int i = threadIdx.x; i <= m; i += blockDim.x) g[i] = i == 0 ? beta : 0.0;
+    if (threadIdx.x == 0) {
+        ctl->j = 0; ctl->it = it; ctl->maxit = maxit; ctl->m = m; ctl->stop = 0;
+        ctl->beta0 = beta0; ctl->tol = tol; ctl->relres = beta / beta0; ctl->hn2 = 0.0; ctl->inv_hn = 0.0;
+    }
+}
+// per-block partial sums of <V_i, w>, i <= ctl->j, into part[block * ldp + i]
+__global__ void __launch_bounds__(256) multidot_ctl(int n, const KryCtl* __restrict__ ctl, int ldp,
+                                                    const double* __restrict__ V, const double* __restrict__ w,
+                                                    double* __restrict__ part) {
+    constexpr int MAXV = 8;
+    __shared__ double red[MAXV][256 / 32];
+    const int nv = ctl->j + 1;
+    for (int i0 = 0; i0 < nv; i0 += MAXV) {
+        const int cnt = min(MAXV, nv - i0);
+        double acc[MAXV];
+#pragma unroll
+        for (int q = 0; q < MAXV; ++q) acc[q] = 0.0;
+        for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+            const double wr = w[r];
+#pragma unroll
+            for (int q = 0; q < MAXV; ++q)
+                if (q < cnt) acc[q] += V[size_t(i0 + q) * n + r] * wr;
+        }
+#pragma unroll
+        for (int q = 0; q < MAXV; ++q) {
+            double a = acc[q];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            double sum = 0.0;
+            for (int q = 0; q < 256 / 32; ++q) sum += red[threadIdx.x][q];
+            part[size_t(blockIdx.x) * ldp + i0 + threadIdx.x] = sum;
+        }
+        __syncthreads();
+    }
+}
+// dots = sum of the partials; column j of H gets them (first pass) or adds them
+__global__ void reduce_parts_ctl(int nblocks, int ldp, const KryCtl* __restrict__ ctl, const double* __restrict__ part,
+                                 double* __restrict__ dots, double* __restrict__ H, int first) {
+    const int nv = ctl->j + 1;
+    double* col = H + size_t(ctl->m + 1) * ctl->j;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        double sum = 0.0;
+        for (int b = 0; b < nblocks; ++b) sum += part[size_t(b) * ldp + i];
+        dots[i] = sum;
+        col[i] = first ? sum : col[i] + sum;
+    }
+}
+// w -= sum_{i <= j} dots[i] V_i
+__global__ void __launch_bounds__(256) basis_update_ctl(int n, const KryCtl* __restrict__ ctl, const double* __restrict__ V,
+                                                        const double* __restrict__ h, double* __restrict__ w) {
+    __shared__ double hs[1024];
+    const int nv = ctl->j + 1;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = h[i];
+    __syncthreads();
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        double sum = w[r];
+        for (int i = 0; i < nv; ++i) sum -= hs[i] * V[size_t(i) * n + r];
+        w[r] = sum;
+    }
+}
+// Givens rotations of column j (FP64), the residual estimate and the loop
+// condition of the cycle's while-node
+__global__ void k_givens(KryCtl* __restrict__ ctl, double* __restrict__ H, double* __restrict__ cs,
+                         double* __restrict__ sn, double* __restrict__ g, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int j = ctl->j, m = ctl->m;
+    double* col = H + size_t(m + 1) * j;
+    const double hn = sqrt(ctl->hn2);
+    col[j + 1] = hn;
+    for (int i = 0; i < j; ++i) {
+        const double a = col[i], c = col[i + 1];
+        col[i] = cs[i] * a + sn[i] * c;
+        col[i + 1] = -sn[i] * a + cs[i] * c;
+    }
+    const double a = col[j], c = col[j + 1];
+    const double d = hypot(a, c);
+    cs[j] = d > 0 ? a / d : 1.0;
+    sn[j] = d > 0 ? c / d : 0.0;
+    col[j] = d;
+    col[j + 1] = 0.0;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    const int jn = j + 1, it = ctl->it + 1;
+    const double relres = fabs(g[jn]) / ctl->beta0;
+    int stop = 0;
+    if (!isfinite(hn) || !isfinite(relres)) stop = 4;
+    else if (relres <= ctl->tol) stop = 1;
+    else if (hn == 0.0) stop = 2;
+    else if (jn >= m || it >= ctl->maxit) stop = 3;
+    ctl->j = jn;
+    ctl->it = it;
+    ctl->relres = relres;
+    ctl->stop = stop;
+    ctl->inv_hn = (stop != 4 && hn > 0.0) ? 1.0 / hn : 0.0;
+    cudaGraphSetConditional(cond, stop ? 0u : 1u);
+}
+// v_{j+1} = w / h(j+1, j) into the basis and into the preconditioner's input
+__global__ void k_scale_next(int n, const KryCtl* __restrict__ ctl, const double* __restrict__ w, double* __restrict__ V,
+                             double* __restrict__ vcur) {
+    const double a = ctl->inv_hn;
+    if (a == 0.0) return;
+    double* vn = V + size_t(ctl->j) * n;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const double v = w[r] * a;
+        vn[r] = v;
+        vcur[r] = v;
+    }
+}
+// y = R^{-1} g for the j x j triangle R of the rotated Hessenberg (one warp).
+// A zero diagonal (an exactly singular least-squares column) contributes a
+// zero coefficient instead of a division by zero.
+__global__ void k_backsolve(const KryCtl* __restrict__ ctl, const double* __restrict__ H, const double* __restrict__ g,
+                            double* __restrict__ y) {
+    const int j = ctl->j, ld = ctl->m + 1, lane = threadIdx.x;
+    for (int i = j - 1; i >= 0; --i) {
+        double part = 0.0;
+        for (int q = i + 1 + lane; q < j; q += 32) part += H[i + size_t(ld) * q] * y[q];
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) {
+            const double dgn = H[i + size_t(ld) * i];
+            y[i] = dgn != 0.0 ? (g[i] - part) / dgn : 0.0;
+        }
+        __syncwarp();
+    }
+}
+
 int vgrid(int n) {
     long b = (long(n) + 255) / 256;
     return int(b < 152 * 4 ? b : 152 * 4);
@@ -184,7 +328,33 @@ struct Krylov {
     void* rhsT = nullptr;    // n, Krylov precision: normalised rhs of an inner solve
     void* xT = nullptr;      // n, Krylov precision: inner solution
     int prec = -1;
+    // device-driven Arnoldi cycle (FP64 Krylov): Hessenberg, rotations and
+    // control block on the device, the cycle as one CUDA graph whose
+    // conditional while-node runs the Arnoldi steps until the control kernel
+    // stops it
+    double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *vcur = nullptr;
+    KryCtl* ctl = nullptr;   // device
+    KryCtl* ctl_pin = nullptr;
+    cudaGraph_t cyc_graph = nullptr;
+    cudaGraphExec_t cyc_exec = nullptr;
+    const void* cyc_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int cyc_full = -1;
+    long long cyc_body_launches = 0;
+    bool cyc_failed = false;   // the runtime refused the conditional graph: host-driven cycles
 };
+
+static void free_krylov(Krylov* k) {
+    if (!k) return;
+    if (k->cyc_exec) cudaGraphExecDestroy(k->cyc_exec);
+    if (k->cyc_graph) cudaGraphDestroy(k->cyc_graph);
+    cudaFree(k->V); cudaFree(k->w); cudaFree(k->z); cudaFree(k->part); cudaFree(k->dots);
+    cudaFree(k->h); cudaFree(k->y); cudaFree(k->r64); cudaFree(k->x64);
+    cudaFree(k->rhsT); cudaFree(k->xT);
+    cudaFree(k->H); cudaFree(k->cs); cudaFree(k->sn); cudaFree(k->g); cudaFree(k->vcur); cudaFree(k->ctl);
+    cudaFreeHost(k->hpin);
+    cudaFreeHost(k->ctl_pin);
+    delete k;
+}
 
 void Engine::spmv64(const double* x, double* y) {
     launch_spmv64(ndim, d_rowptr, d_col, d_val, x, y, stream);
@@ -199,14 +369,8 @@ void Engine::free_solver() {
     delete lu64;
     delete lu32;
     lu64 = lu32 = nullptr;
-    if (kry) {
-        cudaFree(kry->V); cudaFree(kry->w); cudaFree(kry->z); cudaFree(kry->part); cudaFree(kry->dots);
-        cudaFree(kry->h); cudaFree(kry->y); cudaFree(kry->r64); cudaFree(kry->x64);
-        cudaFree(kry->rhsT); cudaFree(kry->xT);
-        cudaFreeHost(kry->hpin);
-        delete kry;
-        kry = nullptr;
-    }
+    free_krylov(kry);
+    kry = nullptr;
     delete ndplan;
     ndplan = nullptr;
 }
@@ -231,13 +395,8 @@ static void ensure_krylov(Engine& e, int m, int prec) {
     Krylov*& k = e.kry;
     const size_t ts = prec ? sizeof(float) : sizeof(double);
     if (k && k->m >= m && k->prec == prec) return;
-    if (k) {
-        cudaFree(k->V); cudaFree(k->w); cudaFree(k->z); cudaFree(k->part); cudaFree(k->dots);
-        cudaFree(k->h); cudaFree(k->y); cudaFree(k->r64); cudaFree(k->x64);
-        cudaFree(k->rhsT); cudaFree(k->xT);
-        cudaFreeHost(k->hpin);
-        delete k;
-    }
+    free_krylov(k);
+    k = nullptr;
     k = new Krylov();
     k->n = e.ndim;
     k->m = m;
@@ -259,7 +418,14 @@ static void ensure_krylov(Engine& e, int m, int prec) {
     k->x64 = static_cast<double*>(A(sizeof(double) * e.ndim));
     k->rhsT = A(ts * e.ndim);
     k->xT = A(ts * e.ndim);
+    k->H = static_cast<double*>(A(sizeof(double) * size_t(m + 1) * m));
+    k->cs = static_cast<double*>(A(sizeof(double) * (m + 1)));
+    k->sn = static_cast<double*>(A(sizeof(double) * (m + 1)));
+    k->g = static_cast<double*>(A(sizeof(double) * (m + 2)));
+    k->vcur = static_cast<double*>(A(sizeof(double) * e.ndim));
+    k->ctl = static_cast<KryCtl*>(A(sizeof(KryCtl)));
     ck(cudaMallocHost(&k->hpin, sizeof(double) * (m + 2)));
+    ck(cudaMallocHost(&k->ctl_pin, sizeof(KryCtl)));
 }
 
 NdLu*& Engine::lu_for(int precision) { return precision == IEMIC_PREC_MIXED ? lu32 : lu64; }
@@ -391,10 +557,11 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
             if (relres <= tol || hn == 0.0) break;
         }
         // y = H^{-1} g (FP64 back substitution), x += M^{-1} (V y)
-        for (int i = j - 1; i >= 0; --i) {
+        for (int i = j - 1; i >= 0; --i) {   // a zero diagonal contributes a zero coefficient
             double sum = g[i];
             for (int q = i + 1; q < j; ++q) sum -= H[size_t(i) * m + q] * y[q];
-            y[i] = sum / H[size_t(i) * m + i];
+            const double dgn = H[size_t(i) * m + i];
+            y[i] = dgn != 0.0 ? sum / dgn : 0.0;
         }
         ck(cudaMemcpyAsync(K.y, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         combine<T><<<G, 256, 0, s>>>(n, j, V, K.y, w); IEMIC_COUNT_LAUNCH();
@@ -406,6 +573,153 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
     ck(cudaGetLastError());
     *relres_out = relres;
     return it;
+}
+
+// The device-driven cycle: one CUDA graph holding a conditional while-node
+// whose body is one Arnoldi step (preconditioner sweeps, SpMV, CGS2, norm,
+// Givens rotation, next basis vector). The step's control kernel updates the
+// residual estimate and ends the loop, so a cycle runs with no host round
+// trip between its iterations. Built once per (factorisation object, matrix,
+// solve mode) and replayed for every cycle and solve.
+static bool ensure_cycle_graph(Engine& e, NdLu& lu, const int* rp, const int* ci, const double* vals) {
+    Krylov& K = *e.kry;
+    const void* key[5] = {&lu, rp, ci, vals, lu.d_factor};
+    const int full = lu.full_inverse ? 1 : 0;
+    if (K.cyc_exec && std::equal(key, key + 5, K.cyc_key) && K.cyc_full == full) return true;
+    if (K.cyc_exec) { cudaGraphExecDestroy(K.cyc_exec); K.cyc_exec = nullptr; }
+    if (K.cyc_graph) { cudaGraphDestroy(K.cyc_graph); K.cyc_graph = nullptr; }
+    cudaStream_t s = e.stream;
+    const int n = e.ndim, G = vgrid(n), m = K.m;
+    double* V = static_cast<double*>(K.V);
+    double* w = static_cast<double*>(K.w);
+    double* z = static_cast<double*>(K.z);
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle cond;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    cudaGraphNode_t node;
+    if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        return false;
+    }
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        return false;
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    ck(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const long long n0 = launch_counter();
+    bool captured = true;
+    try {
+        ndlu_apply(lu, rp, ci, vals, K.vcur, z, 0, s);
+        spmv_csr4<double><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, z, w); IEMIC_COUNT_LAUNCH();
+        for (int pass = 0; pass < 2; ++pass) {   // CGS2
+            multidot_ctl<<<G, 256, 0, s>>>(n, K.ctl, m + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
+            reduce_parts_ctl<<<1, 256, 0, s>>>(G, m + 1, K.ctl, K.part, K.dots, K.H, pass == 0); IEMIC_COUNT_LAUNCH();
+            basis_update_ctl<<<G, 256, 0, s>>>(n, K.ctl, V, K.dots, w); IEMIC_COUNT_LAUNCH();
+        }
+        multidot<double><<<G, 256, 0, s>>>(n, 1, w, w, K.part); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, &K.ctl->hn2, nullptr, 0); IEMIC_COUNT_LAUNCH();
+        k_givens<<<1, 32, 0, s>>>(K.ctl, K.H, K.cs, K.sn, K.g, cond); IEMIC_COUNT_LAUNCH();
+        k_scale_next<<<G, 256, 0, s>>>(n, K.ctl, w, V, K.vcur); IEMIC_COUNT_LAUNCH();
+    } catch (...) {
+        captured = false;
+    }
+    cudaGraph_t out = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &out);
+    K.cyc_body_launches = launch_counter() - n0;
+    launch_counter() = n0;
+    if (!captured || ec != cudaSuccess) {
+        cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        if (!captured) throw EngineError(IEMIC_ERR_CUDA);
+        return false;
+    }
+    if (cudaGraphInstantiate(&K.cyc_exec, g, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        K.cyc_exec = nullptr;
+        (void)cudaGetLastError();
+        return false;
+    }
+    K.cyc_graph = g;
+    std::copy(key, key + 5, K.cyc_key);
+    K.cyc_full = full;
+    return true;
+}
+
+// Restarted GMRES (FP64 Krylov, right preconditioned, x0 = 0) with
+// device-driven cycles; the same iteration as gmres<double> with the
+// Hessenberg, the Givens rotations and the back substitution on the device
+// (FP64). The host waits twice per cycle: for the restart residual and for
+// the cycle's end. Returns false (and does nothing) when the runtime refuses
+// the conditional graph.
+static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const double* vals, const double* b,
+                      double* x, int m, int maxit, double tol, double* relres_out, int* iters_out) {
+    Krylov& K = *e.kry;
+    if (K.cyc_failed) return false;
+    if (!ensure_cycle_graph(e, lu, rp, ci, vals)) {
+        K.cyc_failed = true;
+        return false;
+    }
+    const int n = e.ndim, G = vgrid(n);
+    cudaStream_t s = e.stream;
+    double* V = static_cast<double*>(K.V);
+    double* w = static_cast<double*>(K.w);
+    double* z = static_cast<double*>(K.z);
+    auto norm = [&](const double* a) {
+        multidot<double><<<G, 256, 0, s>>>(n, 1, a, a, K.part); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+        ck(cudaMemcpyAsync(K.hpin, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+        ck(cudaStreamSynchronize(s));
+        return std::sqrt(K.hpin[0]);
+    };
+    ck(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    const double beta0 = norm(b);
+    *iters_out = 0;
+    if (!(beta0 > 0.0)) {
+        *relres_out = 0.0;
+        return true;
+    }
+    if (!std::isfinite(beta0)) throw EngineError(IEMIC_ERR_NAN);
+    int it = 0;
+    double relres = 1.0;
+    for (bool first = true;; first = false) {
+        if (first) {
+            ck(cudaMemcpyAsync(w, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        } else {
+            spmv_csr4<double><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, x, z); IEMIC_COUNT_LAUNCH();
+            sub_from<double><<<G, 256, 0, s>>>(n, b, z, w); IEMIC_COUNT_LAUNCH();
+        }
+        const double beta = norm(w);
+        if (!std::isfinite(beta)) throw EngineError(IEMIC_ERR_NAN);
+        relres = beta / beta0;
+        if (relres <= tol || it >= maxit) break;
+        scale_by<double><<<G, 256, 0, s>>>(n, w, 1.0 / beta, V); IEMIC_COUNT_LAUNCH();
+        ck(cudaMemcpyAsync(K.vcur, V, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        k_cycle_init<<<1, 256, 0, s>>>(K.ctl, K.g, m, beta, beta0, tol, it, maxit); IEMIC_COUNT_LAUNCH();
+        ck(cudaGraphLaunch(K.cyc_exec, s));
+        ck(cudaMemcpyAsync(K.ctl_pin, K.ctl, sizeof(KryCtl), cudaMemcpyDeviceToHost, s));
+        ck(cudaStreamSynchronize(s));
+        const KryCtl c = *K.ctl_pin;
+        launch_counter() += K.cyc_body_launches * (c.it - it);
+        it = c.it;
+        if (c.stop == 4) throw EngineError(IEMIC_ERR_NAN);
+        // y = R^{-1} g, x += M^{-1} (V y)
+        k_backsolve<<<1, 32, 0, s>>>(K.ctl, K.H, K.g, K.y); IEMIC_COUNT_LAUNCH();
+        combine<double><<<G, 256, 0, s>>>(n, c.j, V, K.y, w); IEMIC_COUNT_LAUNCH();
+        ndlu_apply(lu, rp, ci, vals, w, z, 0, s);
+        add_to<double><<<G, 256, 0, s>>>(n, z, x); IEMIC_COUNT_LAUNCH();
+    }
+    ck(cudaGetLastError());
+    *relres_out = relres;
+    *iters_out = it;
+    return true;
 }
 
 int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
@@ -449,7 +763,13 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     if (!fp32_krylov) {
         scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
         double est = 1.0;
-        st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est);
+        int its = 0;
+        if (!timer.on && gmres_dev(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
+                                   &est, &its))
+            st.iters += its;
+        else
+            st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
+                                      &est);
         axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
         residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
         multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();

@@ -2391,6 +2391,24 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
     ck(cudaStreamWaitEvent(s, lu.join_ev, 0));
 }
 
+// Captures the launches of body() on stream s into a new graph. If body()
+// throws, the capture is ended and its partial graph destroyed before the
+// exception propagates, so the stream is never left capturing.
+template <class F>
+static cudaGraph_t capture_graph(cudaStream_t s, F body) {
+    ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+        body();
+    } catch (...) {
+        cudaGraph_t partial = nullptr;
+        if (cudaStreamEndCapture(s, &partial) == cudaSuccess && partial) cudaGraphDestroy(partial);
+        (void)cudaGetLastError();
+        throw;
+    }
+    cudaGraph_t g = nullptr;
+    ck(cudaStreamEndCapture(s, &g));
+    return g;
+}
 // The factorisation is a fixed sequence of ~1,400 launches over buffers that
 // do not move (the CSR arrays of the engine and the factor storage), so it is
 // captured once into a CUDA graph and replayed; with kernel timing on it runs
@@ -2401,15 +2419,19 @@ template <class F>
 static void timed_graph(NdLu& lu, cudaGraphExec_t& exec, std::vector<KTimer::Rec>& tmpl, long long& nlaunch,
                         cudaStream_t s, F body) {
     if (!exec) {
-        cudaGraph_t g = nullptr;
-        ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         const long long n0 = launch_counter();
-        lu.timer->sink = &tmpl;
-        body();
-        lu.timer->sink = nullptr;
+        cudaGraph_t g = capture_graph(s, [&] {
+            lu.timer->sink = &tmpl;
+            try {
+                body();
+            } catch (...) {
+                lu.timer->sink = nullptr;
+                throw;
+            }
+            lu.timer->sink = nullptr;
+        });
         nlaunch = launch_counter() - n0;
         launch_counter() = n0;
-        ck(cudaStreamEndCapture(s, &g));
         const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
         cudaGraphDestroy(g);
         ck(e);
@@ -2422,8 +2444,19 @@ static void timed_graph(NdLu& lu, cudaGraphExec_t& exec, std::vector<KTimer::Rec
 template <class T, int B>
 static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* values, cudaStream_t s) {
     if (lu.timer && lu.timer->on) {
-        if (lu.factor_exec_timed && (lu.fg_rp != rp || lu.fg_ci != ci || lu.fg_val != values))
-            throw EngineError(IEMIC_ERR_STATE);
+        if (lu.factor_exec_timed && (lu.fg_rp != rp || lu.fg_ci != ci || lu.fg_val != values)) {
+            // new CSR buffers: recapture, as the untimed path does; the old
+            // template's events are retired once their records are drained
+            ck(cudaStreamSynchronize(s));
+            lu.timer->drain();
+            cudaGraphExecDestroy(lu.factor_exec_timed);
+            lu.factor_exec_timed = nullptr;
+            for (const KTimer::Rec& r : lu.factor_tmpl) {
+                cudaEventDestroy(r.a);
+                cudaEventDestroy(r.b);
+            }
+            lu.factor_tmpl.clear();
+        }
         lu.fg_rp = rp;
         lu.fg_ci = ci;
         lu.fg_val = values;
@@ -2435,13 +2468,10 @@ static void factor_t(NdLu& lu, const int* rp, const int* ci, const double* value
             lu.factor_exec = nullptr;
         }
         if (!lu.factor_exec) {
-            cudaGraph_t g = nullptr;
-            ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             const long long n0 = launch_counter();
-            factor_body<T, B>(lu, rp, ci, values, s);
+            cudaGraph_t g = capture_graph(s, [&] { factor_body<T, B>(lu, rp, ci, values, s); });
             lu.factor_launches = launch_counter() - n0;
             launch_counter() = n0;
-            ck(cudaStreamEndCapture(s, &g));
             const cudaError_t e = cudaGraphInstantiate(&lu.factor_exec, g, 0);
             cudaGraphDestroy(g);
             ck(e);
@@ -2580,18 +2610,21 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
     const int fm = lu.full_inverse ? 1 : 0;
-    if (kt && kt->on) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    ck(cudaStreamIsCapturing(s, &cap));
+    if (cap == cudaStreamCaptureStatusActive) {
+        // captured into the caller's graph (the device-driven GMRES cycle):
+        // the sweep kernels themselves, not a launch of the sweep graph
+        sweeps_t<T, B>(lu, fm == 1, s);
+    } else if (kt && kt->on) {
         timed_graph(lu, lu.sweep_exec_timed[fm], lu.sweep_tmpl[fm], lu.sweep_launches_timed[fm], s,
                     [&] { sweeps_t<T, B>(lu, fm == 1, s); });
     } else {
         if (!lu.sweep_exec[fm]) {
-            cudaGraph_t g = nullptr;
-            ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             const long long n0 = launch_counter();
-            sweeps_t<T, B>(lu, fm == 1, s);
+            cudaGraph_t g = capture_graph(s, [&] { sweeps_t<T, B>(lu, fm == 1, s); });
             lu.sweep_launches[fm] = launch_counter() - n0;
             launch_counter() = n0;
-            ck(cudaStreamEndCapture(s, &g));
             const cudaError_t e = cudaGraphInstantiate(&lu.sweep_exec[fm], g, 0);
             cudaGraphDestroy(g);
             ck(e);
