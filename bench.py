@@ -16,7 +16,11 @@ metric counts Newton corrector iterations (one Jacobian, three residuals,
 one preconditioner rebuild, the bordered solve(s) and the update each) per
 second of device time. ``--impl reference`` times the CPU restatement of the same
 Newton iteration (C++ oracle assembly + numpy/LAPACK multifrontal LU) on the
-host cores; it is the CPU baseline, not the target.
+host cores; it is the CPU baseline, not the target. The reference arm
+(`--impl reference`) runs the CPU port of the same continuation (restated
+driver, oracle assembly, FP64 multifrontal LU with the reference's
+once-per-step preconditioner) from the committed CPU start state
+tests/golden/start_global96.npz, for at most --ref-steps steps.
 """
 import argparse
 import json
@@ -52,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     ap.add_argument("--cpu-iters", type=int, default=1, help="Newton iterations of the CPU sample")
+    ap.add_argument("--ref-steps", type=int, default=2,
+                    help="continuation steps the reference arm (CPU port) times at most")
     ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1", "newton_large"],
                     help="newton1: one Newton iteration per precision from the seeded state, per-kernel-class "
                          "device times (a short case for profiling); newton_large: Newton iterations on the "
@@ -259,19 +265,92 @@ def cpu_newton_sample(cfg, lm, frc, iters, par_setup):
 
 
 # ---------------------------------------------------------------------------
+def workload_config(args, cfg, nd, par_start, fscale):
+    """The workload description both arms print (computed the same way on
+    the CPU and the GPU side, rounded so that the two agree)."""
+    return {"workload": args.workload, "grid": [cfg["n"], cfg["m"], cfg["l"]], "unknowns": nd,
+            "continuation_parameter": "Salinity Forcing", "setup_combined_forcing": args.setup_comb,
+            "warmup_steps": args.warmup, "start_salinity_forcing": float("%.6g" % par_start),
+            "linear_tol": 1e-8, "newton_tol_abs": float("%.6g" % (1e-8 * fscale)),
+            "preconditioner_policy": "once per step + cost-balanced rebuilds",
+            "parallelism": "replicas", "l2": "working set larger than L2 (factors of 1.5-3 GB per apply)"}
+
+
+START_STATE = os.path.join(REPO, "tests", "golden", "start_global96.npz")
+
+
+def cpu_continuation_sample(args, steps):
+    """The CPU port of the timed continuation: the restated Continuation.H
+    driver (oracle/continuation.py) with the bench's options on the restated
+    THCM model (oracle C++ assembly), solves by the FP64 multifrontal LU on
+    all host cores with the reference's preconditioner policy (a new
+    factorisation once per continuation step, GMRES on it for the step's later
+    Jacobians), from the committed CPU start state at the Salinity Forcing the
+    GPU arm starts from. Returns (cpu_baseline dict, details) or None when the
+    start state is not available for the workload."""
+    import oracle
+    from oracle.continuation import Continuation, MultifrontalModel
+    from oracle.multifrontal import Plan
+    from iemic import workloads as W
+    if args.workload != "global_96x38x12" or not os.path.exists(START_STATE):
+        return None
+    cfg, lm, frc = workload(args.workload)
+    st0 = np.load(START_STATE)
+    o = oracle.Oracle(cfg, lm)
+    names = {"Combined Forcing": "COMB", "Temperature Forcing": "TEMP", "Salinity Forcing": "SALT",
+             "Wind Forcing": "WIND"}
+    for name, v in W.STARTING_PARAMETERS:
+        o.set_par(names[name], v)
+    o.set_par("COMB", 0.0)
+    fscale = float(np.linalg.norm(o.rhs(np.zeros(o.ndim))))
+    o.set_par("COMB", float(st0["combined_forcing"]))
+    par0 = float(st0["salinity_forcing"])
+    o.set_par("SALT", par0)
+    plan = Plan(o.landm(), cfg["n"], cfg["m"], cfg["l"], cfg["periodic"])
+    M = MultifrontalModel(o, plan, policy="step")
+    t0 = time.perf_counter()
+    C = Continuation(M, st0["x"], par="SALT", ds=0.01, ds_min=1e-8, ds_max=0.1, destination=10.0, max_steps=steps,
+                     max_newton=15, min_newton=1, opt_newton=3.5, newton_tol=1e-8 * fscale, residual_test="R",
+                     normalize="N", tangent="S", newton_chord=True, epsilon=1e-5, predictor_bound=3000.0,
+                     tan_scaling=1.0)
+    st = C.run()
+    dt = time.perf_counter() - t0
+    nd = o.ndim
+    o.close()
+    cores = os.cpu_count()
+    warm_note = "" if int(st0["warmup"]) == args.warmup else (
+        " (the committed start state follows %d warm-up steps; this run asked for %d)" % (int(st0["warmup"]),
+                                                                                         args.warmup))
+    sample = ("%d continuation step(s) (%d Newton iterations, %d factorisations, %d GMRES iterations) from "
+              "Salinity Forcing %.6g to %.6g: oracle assembly + FP64 multifrontal LU (numpy/OpenBLAS, %d threads), "
+              "%.1f s%s" % (st["steps"], st["newton_iters"], M.factorizations, M.krylov, par0, C.par, cores, dt,
+                           warm_note))
+    base = {"value": st["newton_iters"] / dt, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    return base, dict(cfg=cfg, nd=nd, par0=par0, fscale=fscale, st=st, dt=dt, par=C.par)
+
+
 def run_reference(args, rank, world):
+    """`--impl reference`: the CPU port of the same continuation
+    (cpu_continuation_sample), at most --ref-steps continuation steps, on
+    rank 0 only."""
     if rank != 0:
         return
-    cfg, lm, frc = workload(args.workload)
-    k = max(1, min(args.steps, 2))
-    base = cpu_newton_sample(cfg, lm, frc, k, args.setup_comb)
-    line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": k,
-            "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded land mask and state)",
-            "config": {"workload": args.workload, "grid": [cfg["n"], cfg["m"], cfg["l"]],
-                       "continuation_parameter": "Salinity Forcing", "tolerance": 1e-8},
-            "impl": "reference", "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    out = cpu_continuation_sample(args, max(1, min(args.steps, args.ref_steps)))
+    if out is None:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU start state of %s is not committed"
+                          % args.workload}), flush=True)
+        return
+    base, d = out
+    st = d["st"]
+    value = base["value"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": st["steps"],
+            "warmup": args.warmup, "ms_per_step": d["dt"] * 1e3 / max(st["steps"], 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded land mask, idealized forcing)",
+            "config": workload_config(args, d["cfg"], d["nd"], d["par0"], d["fscale"]),
+            "impl": "reference", "cpu_baseline": base, "newton_iters": st["newton_iters"],
+            "continuation": {"steps": st["steps"], "failed_steps": st["failed_steps"], "par": d["par"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -391,13 +470,9 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 factors / f64 Krylov+Newton",
         "data": "synthetic (seeded land mask, idealized forcing)",
-        "config": {"workload": args.workload, "grid": [cfg["n"], cfg["m"], cfg["l"]], "unknowns": nd,
-                   "continuation_parameter": "Salinity Forcing", "setup_combined_forcing": args.setup_comb,
-                   "start_salinity_forcing": par_w, "initial_salinity_forcing": salt0,
-                   "linear_tol": 1e-8, "newton_tol_abs": 1e-8 * fscale, "parallelism": "replicas",
-                   "l2": "working set larger than L2: FP32 factors of %.2f GB read per preconditioner apply"
-                         % (4e-9 * info["factor_entries"]),
-                   "factor_gflop": info["factor_flops"] / 1e9, "fronts": info["fronts"]},
+        "config": workload_config(args, cfg, nd, par_w, fscale),
+        "solver": {"factor_gb_fp32": 4e-9 * info["factor_entries"], "factor_gflop": info["factor_flops"] / 1e9,
+                   "fronts": info["fronts"], "start_salinity_forcing": par_w, "initial_salinity_forcing": salt0},
         "newton_iters": mixed["newton_iters"], "continuation": arm_summary(mixed),
         "fp64_gpu": None if fp64 is None else arm_summary(fp64),
         "speedup_vs_fp64_gpu": None if fp64 is None else mixed["value"] / fp64["value"],
@@ -410,7 +485,9 @@ def run_ours(args, rank, world):
         "roofline": roofline(mixed["kstats"], peaks),
     }
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_newton_sample(cfg, lm, frc, args.cpu_iters, args.setup_comb)
+        out = cpu_continuation_sample(args, 1)
+        line["cpu_baseline"] = out[0] if out is not None else cpu_newton_sample(cfg, lm, frc, args.cpu_iters,
+                                                                                  args.setup_comb)
     print(json.dumps(line), flush=True)
 
 

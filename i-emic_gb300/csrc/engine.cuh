@@ -52,6 +52,19 @@ struct Engine {
     int* d_mixflags = nullptr;
     double* d_mixpart = nullptr;
     int any_ocean = 0;
+    // SRES = 0: the integral condition on S in row `rowintcon` (dense over the
+    // S unknowns); "Fix Pressure Points": identity rows rowPfix1/2; -1 if absent
+    int rowintcon = -1, sint_sign = -1, rowPfix1 = -1, rowPfix2 = -1;
+    double* d_intcoef = nullptr;   // cos(y_j) dfzT(k) per cell (0 on land), nc entries
+    // Sherman-Morrison correction of the preconditioner for the dense row,
+    // per factor precision [0] FP64, [1] FP32 factors: zr = M0^{-1} e_r, the
+    // scalar (d.y - y_r) / alpha of the last correction, alpha itself, and
+    // for transposed solves wt = M0^{-T}(d - e_r) with its generation
+    double* d_zr[2] = {nullptr, nullptr};
+    double* d_sm[2] = {nullptr, nullptr};   // [0] alpha, [1] scratch scalar, [2] transposed alpha
+    double* d_wt[2] = {nullptr, nullptr};
+    double* d_smtmp = nullptr;              // scratch vector of the set-up solves
+    long fact_gen[2] = {0, 0}, wt_gen[2] = {-1, -1};
     int *d_rowptr = nullptr, *d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
@@ -88,6 +101,14 @@ struct Engine {
     MixParams mix_params() const;
     // vmix_control before an rhs or jacobian (Mixing = 2); part: 2*152 doubles
     void mix_control(const double* x, double* part);
+    // rows that the Fortran assembly does not produce: the integral condition
+    // and the fixed pressure points (F values after the row kernels)
+    void special_rows_rhs(const double* x, double* F);
+    void zero_mass_rows();
+    // the preconditioner of the dense-row Jacobian: M0^{-1} of the factors
+    // (row rowintcon as an identity row), corrected by Sherman-Morrison
+    void precond_apply(NdLu& lu, int prec, const double* v, double* z, bool transpose);
+    void sm_setup(int prec);
 
     // linear algebra (krylov.cu)
     void spmv64(const double* x, double* y);

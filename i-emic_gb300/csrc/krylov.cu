@@ -36,9 +36,11 @@ namespace {
 
 template <class T>
 __global__ void __launch_bounds__(256) spmv_csr4(int nrows, const int* __restrict__ rp, const int* __restrict__ ci,
-                                                 const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y) {
+                                                 const T* __restrict__ v, const T* __restrict__ x, T* __restrict__ y,
+                                                 int skip) {
     const int lane = threadIdx.x & 3;
     for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; row < nrows; row += (gridDim.x * blockDim.x) >> 2) {
+        if (row == skip) continue;   // the dense row: k_long_row
         const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
         T s = T(0);
         for (int q = b + lane; q < e; q += 4) s += __ldg(v + q) * __ldg(x + __ldg(ci + q));
@@ -51,9 +53,10 @@ __global__ void __launch_bounds__(256) spmv_csr4(int nrows, const int* __restric
 // y = b - J x in FP64
 __global__ void __launch_bounds__(256) residual_csr4(int nrows, const int* __restrict__ rp, const int* __restrict__ ci,
                                                      const double* __restrict__ v, const double* __restrict__ x,
-                                                     const double* __restrict__ b, double* __restrict__ y) {
+                                                     const double* __restrict__ b, double* __restrict__ y, int skip) {
     const int lane = threadIdx.x & 3;
     for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; row < nrows; row += (gridDim.x * blockDim.x) >> 2) {
+        if (row == skip) continue;
         const int s0 = __ldg(rp + row), e = __ldg(rp + row + 1);
         double s = 0.0;
         for (int q = s0 + lane; q < e; q += 4) s += __ldg(v + q) * __ldg(x + __ldg(ci + q));
@@ -62,6 +65,62 @@ __global__ void __launch_bounds__(256) residual_csr4(int nrows, const int* __res
         if (lane == 0) y[row] = b[row] - s;
     }
 }
+
+// One long CSR row (the dense integral-condition row) as a block-wide
+// reduction: y[row] = (b[row] if b) - sum_q v[q] x[ci[q]]... or + the sum.
+template <class T>
+__global__ void __launch_bounds__(1024) k_long_row(const int* __restrict__ rp, const int* __restrict__ ci,
+                                                   const T* __restrict__ v, const T* __restrict__ x,
+                                                   const double* __restrict__ b, T* __restrict__ y, int row) {
+    __shared__ double red[1024];
+    double sum = 0.0;
+    for (int q = rp[row] + threadIdx.x; q < rp[row + 1]; q += blockDim.x) sum += double(v[q]) * double(x[ci[q]]);
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) y[row] = b ? T(b[row] - red[0]) : T(red[0]);
+}
+// Sherman-Morrison scalars of the dense row d (row `row` of J):
+//   mode 0: out = (d.z - z_row) / sm[0]          (the forward correction)
+//   mode 1: out = 1 + d.z - z_row                (alpha, from z = M0^{-1} e_row)
+//   mode 2: out = z_row / sm[2]                  (the transposed correction)
+//   mode 3: out = 1 + z_row                      (transposed alpha, z = M0^{-T}(d - e_row))
+__global__ void __launch_bounds__(1024) k_sm_scalar(const int* __restrict__ rp, const int* __restrict__ ci,
+                                                    const double* __restrict__ v, const double* __restrict__ z, int row,
+                                                    const double* __restrict__ sm, double* __restrict__ out, int mode) {
+    __shared__ double red[1024];
+    double sum = 0.0;
+    if (mode <= 1)
+        for (int q = rp[row] + threadIdx.x; q < rp[row + 1]; q += blockDim.x) sum += v[q] * z[ci[q]];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double zr = z[row];
+        if (mode == 0) out[0] = (red[0] - zr) / sm[0];
+        else if (mode == 1) out[0] = 1.0 + red[0] - zr;
+        else if (mode == 2) out[0] = zr / sm[2];
+        else out[0] = 1.0 + zr;
+    }
+}
+// z -= scal[0] * w
+__global__ void k_axpy_scal(int n, const double* __restrict__ scal, const double* __restrict__ w, double* __restrict__ z) {
+    const double a = scal[0];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) z[r] -= a * w[r];
+}
+// out = d - e_row as a vector (d: the entries of CSR row `row`)
+__global__ void k_row_vector(const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ v, int row,
+                             double* __restrict__ out) {
+    for (int q = rp[row] + blockIdx.x * blockDim.x + threadIdx.x; q < rp[row + 1]; q += gridDim.x * blockDim.x)
+        out[ci[q]] = v[q] - (ci[q] == row ? 1.0 : 0.0);
+}
+__global__ void k_set_unit(double* __restrict__ v, int row) { v[row] = 1.0; }
 
 // partial sums of dots[i] = <V_i, w>, i < nv, per block (double partials)
 template <class T>
@@ -305,11 +364,29 @@ int spmv_grid(int nrows) {
 
 }  // namespace
 
-void launch_spmv64(int nrows, const int* rp, const int* ci, const double* v, const double* x, double* y, cudaStream_t s) {
-    spmv_csr4<double><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y); IEMIC_COUNT_LAUNCH();
+// y = A x with A in CSR; row `skip` (a dense row, or -1) by a block-wide reduction
+template <class T>
+static void spmv_launch(int nrows, const int* rp, const int* ci, const T* v, const T* x, T* y, int skip, cudaStream_t s) {
+    spmv_csr4<T><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y, skip); IEMIC_COUNT_LAUNCH();
+    if (skip >= 0) {
+        k_long_row<T><<<1, 1024, 0, s>>>(rp, ci, v, x, nullptr, y, skip); IEMIC_COUNT_LAUNCH();
+    }
 }
-void launch_spmv32(int nrows, const int* rp, const int* ci, const float* v, const float* x, float* y, cudaStream_t s) {
-    spmv_csr4<float><<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, y); IEMIC_COUNT_LAUNCH();
+// y = b - A x
+static void residual_launch(int nrows, const int* rp, const int* ci, const double* v, const double* x, const double* b,
+                            double* y, int skip, cudaStream_t s) {
+    residual_csr4<<<spmv_grid(nrows), 256, 0, s>>>(nrows, rp, ci, v, x, b, y, skip); IEMIC_COUNT_LAUNCH();
+    if (skip >= 0) {
+        k_long_row<double><<<1, 1024, 0, s>>>(rp, ci, v, x, b, y, skip); IEMIC_COUNT_LAUNCH();
+    }
+}
+void launch_spmv64(int nrows, const int* rp, const int* ci, const double* v, const double* x, double* y, int skip,
+                   cudaStream_t s) {
+    spmv_launch<double>(nrows, rp, ci, v, x, y, skip, s);
+}
+void launch_spmv32(int nrows, const int* rp, const int* ci, const float* v, const float* x, float* y, int skip,
+                   cudaStream_t s) {
+    spmv_launch<float>(nrows, rp, ci, v, x, y, skip, s);
 }
 
 // Krylov workspace (both precisions share the layout)
@@ -357,11 +434,11 @@ static void free_krylov(Krylov* k) {
 }
 
 void Engine::spmv64(const double* x, double* y) {
-    launch_spmv64(ndim, d_rowptr, d_col, d_val, x, y, stream);
+    launch_spmv64(ndim, d_rowptr, d_col, d_val, x, y, rowintcon, stream);
     ck(cudaGetLastError());
 }
 void Engine::spmv32(const float* x, float* y) {
-    launch_spmv32(ndim, d_rowptr, d_col, d_val32, x, y, stream);
+    launch_spmv32(ndim, d_rowptr, d_col, d_val32, x, y, rowintcon, stream);
     ck(cudaGetLastError());
 }
 
@@ -378,7 +455,8 @@ void Engine::free_solver() {
 void Engine::ensure_solver() {
     if (!ndplan) {
         ndplan = new NdPlan();
-        build_nd_plan(*ndplan, cfg.n, cfg.m, cfg.l, cfg.periodic ? 1 : 0, landm, row_ptr, host_col_idx(), 32);
+        build_nd_plan(*ndplan, cfg.n, cfg.m, cfg.l, cfg.periodic ? 1 : 0, landm, row_ptr, host_col_idx(), 32,
+                      {rowintcon, rowPfix1, rowPfix2}, {rowPfix1, rowPfix2});
     }
 }
 
@@ -443,6 +521,56 @@ void Engine::build_preconditioner(int precision) {
     ck(cudaStreamSynchronize(stream));
     timer.drain();
     if (precision == IEMIC_PREC_MIXED) fact32_stale = false; else fact64_stale = false;
+    sm_setup(precision == IEMIC_PREC_MIXED ? 1 : 0);
+}
+
+// Dense integral-condition row r (SRES = 0): the factorisation treats row r
+// as the identity row e_r (J0 = J + e_r (e_r - d)^T, d = row r of J), which
+// keeps its elimination tree local, and the preconditioner restores d by
+// Sherman-Morrison:
+//   J^{-1} v  = y - zr (d.y - y_r) / alpha,   y = M0^{-1} v, zr = M0^{-1} e_r,
+//               alpha = 1 + d.zr - zr_r
+//   J^{-T} v  = y - wt y_r / (1 + wt_r),       y = M0^{-T} v, wt = M0^{-T} (d - e_r)
+// zr and alpha are refreshed after every factorisation, wt on the first
+// transposed solve of a factorisation.
+void Engine::sm_setup(int pi) {
+    ++fact_gen[pi];
+    if (rowintcon < 0) return;
+    NdLu* lu = pi ? lu32 : lu64;
+    if (!d_zr[pi]) {
+        d_zr[pi] = static_cast<double*>(dalloc(sizeof(double) * ndim));
+        d_sm[pi] = static_cast<double*>(dalloc(sizeof(double) * 4));
+    }
+    if (!d_smtmp) d_smtmp = static_cast<double*>(dalloc(sizeof(double) * ndim));
+    ck(cudaMemsetAsync(d_smtmp, 0, sizeof(double) * ndim, stream));
+    k_set_unit<<<1, 1, 0, stream>>>(d_smtmp, rowintcon); IEMIC_COUNT_LAUNCH();
+    ndlu_apply(*lu, d_rowptr, d_col, d_val, d_smtmp, d_zr[pi], 0, stream);
+    k_sm_scalar<<<1, 1024, 0, stream>>>(d_rowptr, d_col, d_val, d_zr[pi], rowintcon, d_sm[pi], d_sm[pi], 1); IEMIC_COUNT_LAUNCH();
+    ck(cudaGetLastError());
+}
+
+void Engine::precond_apply(NdLu& lu, int pi, const double* v, double* z, bool transpose) {
+    cudaStream_t s = stream;
+    if (!transpose) {
+        ndlu_apply(lu, d_rowptr, d_col, d_val, v, z, 0, s);
+        if (rowintcon < 0) return;
+        k_sm_scalar<<<1, 1024, 0, s>>>(d_rowptr, d_col, d_val, z, rowintcon, d_sm[pi], d_sm[pi] + 1, 0); IEMIC_COUNT_LAUNCH();
+        k_axpy_scal<<<vgrid(ndim), 256, 0, s>>>(ndim, d_sm[pi] + 1, d_zr[pi], z); IEMIC_COUNT_LAUNCH();
+        return;
+    }
+    if (rowintcon >= 0 && wt_gen[pi] != fact_gen[pi]) {
+        if (!d_wt[pi]) d_wt[pi] = static_cast<double*>(dalloc(sizeof(double) * ndim));
+        if (!d_smtmp) d_smtmp = static_cast<double*>(dalloc(sizeof(double) * ndim));
+        ck(cudaMemsetAsync(d_smtmp, 0, sizeof(double) * ndim, s));
+        k_row_vector<<<vgrid(ndim), 256, 0, s>>>(d_rowptr, d_col, d_val, rowintcon, d_smtmp); IEMIC_COUNT_LAUNCH();
+        ndlu_apply_transpose(lu, d_smtmp, d_wt[pi], s);
+        k_sm_scalar<<<1, 1024, 0, s>>>(d_rowptr, d_col, d_val, d_wt[pi], rowintcon, d_sm[pi], d_sm[pi] + 2, 3); IEMIC_COUNT_LAUNCH();
+        wt_gen[pi] = fact_gen[pi];
+    }
+    ndlu_apply_transpose(lu, v, z, s);
+    if (rowintcon < 0) return;
+    k_sm_scalar<<<1, 1024, 0, s>>>(d_rowptr, d_col, d_val, z, rowintcon, d_sm[pi], d_sm[pi] + 3, 2); IEMIC_COUNT_LAUNCH();
+    k_axpy_scal<<<vgrid(ndim), 256, 0, s>>>(ndim, d_sm[pi] + 3, d_wt[pi], z); IEMIC_COUNT_LAUNCH();
 }
 
 void Engine::apply_precon(int precision, const double* v, double* out) {
@@ -450,7 +578,7 @@ void Engine::apply_precon(int precision, const double* v, double* out) {
     if (!lu || !lu->factored) throw EngineError(IEMIC_ERR_STATE);
     // FP64 vectors in and out for both factor precisions (the mixed solve
     // applies its FP32 factors to FP64 Krylov vectors the same way)
-    ndlu_apply(*lu, d_rowptr, d_col, d_val, v, out, 0, stream);
+    precond_apply(*lu, precision == IEMIC_PREC_MIXED ? 1 : 0, v, out, false);
     ck(cudaGetLastError());
 }
 
@@ -458,10 +586,8 @@ void Engine::apply_precon(int precision, const double* v, double* out) {
 template <class T>
 static void precond(NdLu& lu, Engine& e, const T* v, T* z, bool transpose, cudaStream_t s) {
     if constexpr (sizeof(T) == 8) {
-        if (transpose) {
-            ndlu_apply_transpose(lu, v, z, s);
-            return;
-        }
+        e.precond_apply(lu, &lu == e.lu32 ? 1 : 0, v, z, transpose);
+        return;
     }
     ndlu_apply(lu, e.d_rowptr, e.d_col, e.d_val, v, z, sizeof(T) == 4, s);
 }
@@ -471,7 +597,7 @@ static void precond(NdLu& lu, Engine& e, const T* v, T* z, bool transpose, cudaS
 // workspace. Returns the inner iterations used.
 template <class T>
 static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* vals, const T* b, T* x, int m, int maxit,
-                 double tol, double* relres_out, bool transpose = false) {
+                 double tol, double* relres_out, bool transpose = false, int skip = -1) {
     Krylov& K = *e.kry;
     const int n = e.ndim;
     cudaStream_t s = e.stream;
@@ -504,7 +630,7 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
         if (first) {
             ck(cudaMemcpyAsync(w, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
         } else {
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, x, z); IEMIC_COUNT_LAUNCH();
+            spmv_launch<T>(n, rp, ci, vals, x, z, skip, s);
             sub_from<T><<<G, 256, 0, s>>>(n, b, z, w); IEMIC_COUNT_LAUNCH();
         }
         first = false;
@@ -519,7 +645,7 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
         for (; j < m && it < maxit;) {
             precond(lu, e, V + size_t(j) * n, z, transpose, s);
             cudaEvent_t ev = e.timer.start(s);
-            spmv_csr4<T><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, z, w); IEMIC_COUNT_LAUNCH();
+            spmv_launch<T>(n, rp, ci, vals, z, w, skip, s);
             e.timer.stop(ev, s, IEMIC_KC_SPMV, spmv_bytes, 2.0 * double(e.nnz));
             for (int pass = 0; pass < 2; ++pass) {   // CGS2
                 multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
@@ -617,8 +743,8 @@ static bool ensure_cycle_graph(Engine& e, NdLu& lu, const int* rp, const int* ci
     const long long n0 = launch_counter();
     bool captured = true;
     try {
-        ndlu_apply(lu, rp, ci, vals, K.vcur, z, 0, s);
-        spmv_csr4<double><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, z, w); IEMIC_COUNT_LAUNCH();
+        e.precond_apply(lu, &lu == e.lu32 ? 1 : 0, K.vcur, z, false);
+        spmv_launch<double>(n, rp, ci, vals, z, w, e.rowintcon, s);
         for (int pass = 0; pass < 2; ++pass) {   // CGS2
             multidot_ctl<<<G, 256, 0, s>>>(n, K.ctl, m + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
             reduce_parts_ctl<<<1, 256, 0, s>>>(G, m + 1, K.ctl, K.part, K.dots, K.H, pass == 0); IEMIC_COUNT_LAUNCH();
@@ -693,7 +819,7 @@ static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const d
         if (first) {
             ck(cudaMemcpyAsync(w, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         } else {
-            spmv_csr4<double><<<spmv_grid(n), 256, 0, s>>>(n, rp, ci, vals, x, z); IEMIC_COUNT_LAUNCH();
+            spmv_launch<double>(n, rp, ci, vals, x, z, e.rowintcon, s);
             sub_from<double><<<G, 256, 0, s>>>(n, b, z, w); IEMIC_COUNT_LAUNCH();
         }
         const double beta = norm(w);
@@ -713,7 +839,7 @@ static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const d
         // y = R^{-1} g, x += M^{-1} (V y)
         k_backsolve<<<1, 32, 0, s>>>(K.ctl, K.H, K.g, K.y); IEMIC_COUNT_LAUNCH();
         combine<double><<<G, 256, 0, s>>>(n, c.j, V, K.y, w); IEMIC_COUNT_LAUNCH();
-        ndlu_apply(lu, rp, ci, vals, w, z, 0, s);
+        e.precond_apply(lu, &lu == e.lu32 ? 1 : 0, w, z, false);
         add_to<double><<<G, 256, 0, s>>>(n, z, x); IEMIC_COUNT_LAUNCH();
     }
     ck(cudaGetLastError());
@@ -769,9 +895,9 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
             st.iters += its;
         else
             st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
-                                      &est);
+                                      &est, false, rowintcon);
         axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
-        residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+        residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
         multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
         reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
         double rn2 = 0.0;
@@ -792,9 +918,10 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
             convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm); IEMIC_COUNT_LAUNCH();
             double est = 1.0;
             double inner = std::max(o.inner_tol, 0.5 * o.tol / relres);
-            st.iters += gmres<float>(*this, *lu, d_rowptr, d_col, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner, &est);
+            st.iters += gmres<float>(*this, *lu, d_rowptr, d_col, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner,
+                                     &est, false, rowintcon);
             axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x); IEMIC_COUNT_LAUNCH();
-            residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowptr, d_col, d_val, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+            residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
             multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
             reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
             double rn2 = 0.0;
@@ -888,7 +1015,7 @@ int Engine::solve_transpose_dev(const double* b, double* x, const iemic_solve_op
     st.iters += gmres<double>(*this, *lu, d_rowT, d_colT, d_valT, K.r64, K.x64, o.restart, o.max_iters, o.tol, &est,
                               true);
     axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
-    residual_csr4<<<spmv_grid(n), 256, 0, s>>>(n, d_rowT, d_colT, d_valT, x, b, K.r64); IEMIC_COUNT_LAUNCH();
+    residual_launch(n, d_rowT, d_colT, d_valT, x, b, K.r64, -1, s);
     multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
     reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double rn2 = 0.0;

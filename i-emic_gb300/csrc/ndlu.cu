@@ -49,7 +49,8 @@ struct Node {
 }  // namespace
 
 void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::vector<int>& landm,
-                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel) {
+                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel,
+                   const std::vector<int>& identity_rows, const std::vector<int>& fixed_pressures) {
     plan = NdPlan();
     plan.panel = panel;
     const int ndim = NUN * n * m * l;
@@ -73,6 +74,10 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
                 }
                 if (LM(i, j, k + 1) == LAND) dry[base + 2] = 1;
             }
+    // rows the factorisation takes as identity rows: the integral condition
+    // (its dense row is restored by the solve phase's Sherman-Morrison step)
+    for (int r : identity_rows)
+        if (r >= 0 && r < ndim) dry[r] = 1;
     // 2. barotropic pressure of every water column. A column's pressures are
     //    tied together by its hydrostatic w rows, so one pressure per column (at
     //    the surface) carries its depth-independent mode; that mode couples
@@ -139,6 +144,15 @@ void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::v
             dpinned[dfind(c)] = 1;
             plan.pins.push_back(grow(c % n, c / n, l - 1, PP - 1));
         };
+        // surface pressures the model itself fixes ("Fix Pressure Points":
+        // identity rows of J, passed in identity_rows) already remove the
+        // null modes of their components: no gauge pin there
+        for (int r : fixed_pressures) {
+            if (r < 0 || r >= ndim || r % NUN != PP - 1) continue;
+            const int cell = r / NUN, ci0 = cell % n, cj0 = (cell / n) % m, ck0 = cell / (n * m);
+            if (ck0 != l - 1 || !ocean_col[ci0 + n * cj0]) continue;
+            dpinned[dfind(ci0 + n * cj0)] = 1;
+        }
         std::vector<std::vector<int>> comps(size_t(n) * m);
         for (int j = m - 1; j >= 0; --j)      // scan from the north-east corner
             for (int i = n - 1; i >= 0; --i)

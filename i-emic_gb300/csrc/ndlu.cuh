@@ -58,7 +58,8 @@ struct NdPlan {
 // consistency of a plan's offsets and indices (throws IEMIC_ERR_STATE)
 void check_nd_plan(const NdPlan& plan);
 void build_nd_plan(NdPlan& plan, int n, int m, int l, int periodic, const std::vector<int>& landm,
-                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel);
+                   const std::vector<int>& row_ptr, const std::vector<int>& col_idx, int panel,
+                   const std::vector<int>& identity_rows = {}, const std::vector<int>& fixed_pressures = {});
 
 // Device-resident factorisation for one precision.
 struct NdLu {

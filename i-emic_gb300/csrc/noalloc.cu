@@ -63,6 +63,7 @@ extern "C" int iemic_rhs_dev_noalloc(iemic_ocean* h, const double* x_dev, double
         launch_usol(e.geo, x_dev, pads, e.stream);
         e.mix_control(x_dev, pads + 5 * kMaxPadded);
         launch_rhs(e.geo, e.P, mp, e.fs, e.d_al, pads, x_dev, e.d_surf, F_dev, e.stream);
+        e.special_rows_rhs(x_dev, F_dev);   // integral condition / fixed pressures: shared memory only
     } catch (const EngineError& err) {
         return err.code;
     }

@@ -205,6 +205,24 @@ void Engine::update_forcing() {
     fs.hmtp = p[HMTP];
     fs.sper_fac = p[SPER] * (double(1 - cfg.sres) + cfg.sres * p[BIOT]);
     fs.temcor = fs.salcor = fs.adapted_salcor = fs.spertcor = 0.0;
+    // qint (src/ocean/forcing.F90:452-464, THCM.C:2653-2686): with no
+    // restoring the area mean of the surface flux is removed
+    auto qint = [&](int f) {
+        double lfsint = 0.0, lsint = 0.0;
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int lmv = LMs(i + 1, j + 1);
+                lfsint = surf[size_t(f) * nm + size_t(i) + size_t(n) * j] * std::cos(y[j + 1]) * double(1 - lmv) + lfsint;
+                lsint = std::cos(y[j + 1]) * double(1 - lmv) + lsint;
+            }
+        return lfsint / lsint;
+    };
+    if (cfg.ite == 1 && cfg.tres == 0) fs.temcor = qint(2);
+    if (cfg.sres == 0) {
+        if (cfg.its == 1) fs.salcor = qint(3);
+        fs.adapted_salcor = 0.0;   // adapted_emip is zero here: its mean is zero
+        fs.spertcor = qint(4);
+    }
     ck(cudaMemcpyAsync(d_surf, surf.data(), sizeof(double) * surf.size(), cudaMemcpyHostToDevice, stream));
 }
 
@@ -245,6 +263,7 @@ void Engine::build_pattern() {
                 size_t r0 = size_t(NUN) * (i + size_t(n) * (j + size_t(m) * k));
                 for (int A = 1; A <= 6; ++A) row_ptr[r0 + A] = len[size_t(cls) * 7 + A];
             }
+    if (rowintcon >= 0) row_ptr[size_t(rowintcon) + 1] = int(nc);   // the dense integral-condition row
     for (size_t r = 0; r < size_t(ndim); ++r) row_ptr[r + 1] += row_ptr[r];
     nnz = row_ptr[ndim];
 }
@@ -290,6 +309,16 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
         if (v != OCEAN && v != LAND) throw EngineError(IEMIC_ERR_ARG);
     }
     build_grid();
+    if (c.sres == 0) {   // location of the integral condition (THCM.C:651-697)
+        const int Nic = c.intcon_i >= 0 ? c.intcon_i : n - 1, Mic = c.intcon_j >= 0 ? c.intcon_j : m - 1;
+        if (Nic >= n || Mic >= m || LM(Nic + 1, Mic + 1, l) != OCEAN) throw EngineError(IEMIC_ERR_ARG);
+        rowintcon = NUN * ((l - 1) * n * m + n * Mic + Nic) + SS - 1;
+        sint_sign = c.sint_sign == 0 ? -1 : c.sint_sign;
+    }
+    if (c.fix_pressure_points) {   // THCM.C:749-758
+        rowPfix1 = NUN * ((l - 1) * n * m + n * (m - 1) + (n - 1)) + PP - 1;
+        rowPfix2 = NUN * ((l - 1) * n * m + n * (m - 1) + (n - 2)) + PP - 1;
+    }
     stpnt();
     // device data
     std::vector<int8_t> lm8(nl);
@@ -324,12 +353,24 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
     ck(cudaMemcpyAsync(d_slot, slot.data(), slot.size(), cudaMemcpyHostToDevice, stream));
     pat.row_ptr = d_rowptr; pat.col_idx = d_col; pat.slot = d_slot;
     launch_pattern(geo, pat, d_col, stream);
+    if (rowintcon >= 0) launch_dense_row_cols(int(nc), d_col + row_ptr[rowintcon], stream);
+    // intcond_scaling (src/ocean/thcm_utils.F90:285-312): cos(y_j) dfzT(k) on ocean cells
+    d_intcoef = static_cast<double*>(dalloc(sizeof(double) * nc));
+    {
+        std::vector<double> coef(nc, 0.0);
+        for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+            if (LM(i, j, k) == OCEAN)
+                coef[size_t(i - 1) + size_t(n) * (size_t(j - 1) + size_t(m) * (k - 1))] = std::cos(y[j]) * dfzT[k];
+        ck(cudaMemcpyAsync(d_intcoef, coef.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, stream));
+        ck(cudaStreamSynchronize(stream));
+    }
     ck(cudaGetLastError());
     ck(cudaMemsetAsync(d_val, 0, sizeof(double) * size_t(nnz), stream));
     ck(cudaMemsetAsync(d_val32, 0, sizeof(float) * size_t(nnz), stream));
     update_forcing();
     lin();
     launch_mass(geo, P, d_B, stream);
+    zero_mass_rows();
     ck(cudaGetLastError());
     // vmix_init (src/ocean/mix_imp.f:57-111): Mixing = 1 fixes the partition
     // of T and S rows and columns; Mixing = 2 starts with both fields off
@@ -358,10 +399,21 @@ MixParams Engine::mix_params() const {
     return M;
 }
 
+void Engine::special_rows_rhs(const double* x, double* F) {
+    launch_special_rhs(int(nc), d_intcoef, x, F, rowintcon, sint_sign, rowPfix1, rowPfix2, stream);
+}
+
 // Ocean::computeRHS / computeJacobian call THCM::fixMixing(0) (Ocean.C:1281,
 // 1302), so with Mixing = 2 every evaluation re-runs vmix_control.
 void Engine::mix_control(const double* x, double* part) {
     if (cfg.vmix == 2) launch_mix_control(geo, x, part, d_mixflags, any_ocean, stream);
+}
+
+// B is zero in the rows that carry no time derivative: the integral
+// condition (assemble.F90:49, THCM.C:1233-1238) and the fixed pressure points
+void Engine::zero_mass_rows() {
+    for (int r : {rowintcon, rowPfix1, rowPfix2})
+        if (r >= 0) ck(cudaMemsetAsync(d_B + r, 0, sizeof(double), stream));
 }
 
 void Engine::set_par(int idx, double value) {
@@ -369,6 +421,7 @@ void Engine::set_par(int idx, double value) {
     update_forcing();
     lin();
     launch_mass(geo, P, d_B, stream);
+    zero_mass_rows();
     ck(cudaGetLastError());
     jac_valid = false;
 }
@@ -382,6 +435,7 @@ void Engine::rhs_dev(const double* x, double* F) {
     launch_usol(geo, x, d_pads, stream);
     mix_control(x, d_mixpart);
     launch_rhs(geo, P, mp, fs, d_al, d_pads, x, d_surf, F, stream);
+    special_rows_rhs(x, F);
     timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 8.0 * 4.0 * ndim, 0.0);
     ck(cudaGetLastError());
 }
@@ -392,6 +446,8 @@ void Engine::jacobian_dev(const double* x) {
     launch_usol(geo, x, d_pads, stream);
     mix_control(x, d_mixpart);
     launch_jacobian(geo, P, mp, pat, d_al, d_pads, d_val, d_val32, stream);
+    launch_special_jac(int(nc), d_rowptr, d_col, d_intcoef, d_val, d_val32, rowintcon, sint_sign, rowPfix1, rowPfix2,
+                       stream);
     timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 12.0 * double(nnz) + 8.0 * 3.0 * ndim, 0.0);
     ck(cudaGetLastError());
     jac_valid = true;

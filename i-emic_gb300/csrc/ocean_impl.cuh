@@ -93,5 +93,11 @@ void launch_rhs(const Geo& g, const Params& p, const MixParams& mp, const Forcin
 // of the state (part: 2 * 152 doubles of scratch) and the flag update.
 void launch_mix_control(const Geo& g, const double* x, double* part, int* flags, int any_ocean, cudaStream_t s);
 void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s);
+// the integral-condition row (SRES = 0) and the fixed pressure points
+void launch_special_rhs(int nc, const double* coef, const double* x, double* F, int row, int sign, int pfix1, int pfix2,
+                        cudaStream_t s);
+void launch_special_jac(int nc, const int* rp, const int* ci, const double* coef, double* val, float* val32, int row,
+                        int sign, int pfix1, int pfix2, cudaStream_t s);
+void launch_dense_row_cols(int nc, int* cols, cudaStream_t s);
 
 }  // namespace iemic

@@ -948,10 +948,76 @@ void launch_rhs(const Geo& g, const Params& p, const MixParams& mp, const Forcin
     size_t blocks = (nc + 31) / 32;
     rhs_kernel<<<int(blocks), 192, 0, s>>>(g, p, mp, fs, al_tab, pads, x, surf, F); IEMIC_COUNT_LAUNCH();
 }
+// Rows the Fortran assembly does not produce (THCM::evaluate, src/ocean/THCM.C:
+// 1014-1041): the integral condition F_r = sign * sum_cells coef_c S_c
+// (one block; tree reduction in shared memory, no global scratch) and the
+// fixed pressure points F = 0.
+__global__ void __launch_bounds__(1024) k_special_rhs(int nc, const double* __restrict__ coef,
+                                                      const double* __restrict__ x, double* __restrict__ F, int row,
+                                                      int sign, int pfix1, int pfix2) {
+    __shared__ double red[1024];
+    double sum = 0.0;
+    if (row >= 0)
+        for (int c = threadIdx.x; c < nc; c += blockDim.x) sum += coef[c] * x[size_t(NUN) * c + SS - 1];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (row >= 0) F[row] = sign * (red[0] - 0.0);
+        if (pfix1 >= 0) F[pfix1] = 0.0;
+        if (pfix2 >= 0) F[pfix2] = 0.0;
+    }
+}
+// Jacobian rows the assembly does not produce: the dense integral-condition
+// row (its columns are the S unknowns of every cell, in order) and the
+// identity rows of the fixed pressure points.
+__global__ void k_special_jac(int nc, const int* __restrict__ rp, const int* __restrict__ ci,
+                              const double* __restrict__ coef, double* __restrict__ val, float* __restrict__ val32,
+                              int row, int sign, int pfix1, int pfix2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= 0)
+        for (int c = t; c < nc; c += gridDim.x * blockDim.x) {
+            const double v = sign * coef[c];
+            val[rp[row] + c] = v;
+            if (val32) val32[rp[row] + c] = float(v);
+        }
+    const int pf[2] = {pfix1, pfix2};
+    if (t == 0)
+        for (int k = 0; k < 2; ++k) {
+            const int r = pf[k];
+            if (r < 0) continue;
+            for (int q = rp[r]; q < rp[r + 1]; ++q) {
+                const double v = ci[q] == r ? 1.0 : 0.0;
+                val[q] = v;
+                if (val32) val32[q] = float(v);
+            }
+        }
+}
+__global__ void k_dense_row_cols(int nc, int* __restrict__ cols) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x)
+        cols[c] = NUN * c + SS - 1;
+}
 void launch_mix_control(const Geo& g, const double* x, double* part, int* flags, int any_ocean, cudaStream_t s) {
     mix_norm_part<<<152, 256, 0, s>>>(g, x, part); IEMIC_COUNT_LAUNCH();
     mix_control<<<1, 32, 0, s>>>(part, 152, flags, any_ocean); IEMIC_COUNT_LAUNCH();
 }
+void launch_special_rhs(int nc, const double* coef, const double* x, double* F, int row, int sign, int pfix1, int pfix2,
+                        cudaStream_t s) {
+    if (row < 0 && pfix1 < 0 && pfix2 < 0) return;
+    k_special_rhs<<<1, 1024, 0, s>>>(nc, coef, x, F, row, sign, pfix1, pfix2); IEMIC_COUNT_LAUNCH();
+}
+void launch_special_jac(int nc, const int* rp, const int* ci, const double* coef, double* val, float* val32, int row,
+                        int sign, int pfix1, int pfix2, cudaStream_t s) {
+    if (row < 0 && pfix1 < 0 && pfix2 < 0) return;
+    k_special_jac<<<grid_for(size_t(nc), 256), 256, 0, s>>>(nc, rp, ci, coef, val, val32, row, sign, pfix1, pfix2); IEMIC_COUNT_LAUNCH();
+}
+void launch_dense_row_cols(int nc, int* cols, cudaStream_t s) {
+    k_dense_row_cols<<<grid_for(size_t(nc), 256), 256, 0, s>>>(nc, cols); IEMIC_COUNT_LAUNCH();
+}
+
 void launch_mass(const Geo& g, const Params& p, double* diagB, cudaStream_t s) {
     size_t nc = size_t(g.n) * g.m * g.l;
     mass_kernel<<<grid_for(nc, 256), 256, 0, s>>>(g, p.par[ROSB], diagB); IEMIC_COUNT_LAUNCH();

@@ -47,7 +47,8 @@ class Config(ctypes.Structure):
                 ("tres", ctypes.c_int), ("sres", ctypes.c_int),
                 ("iza", ctypes.c_int), ("ite", ctypes.c_int), ("its", ctypes.c_int),
                 ("forcing_type", ctypes.c_int), ("vmix", ctypes.c_int), ("rho_mixing", ctypes.c_int),
-                ("tap", ctypes.c_int)]
+                ("tap", ctypes.c_int), ("sint_sign", ctypes.c_int), ("intcon_i", ctypes.c_int),
+                ("intcon_j", ctypes.c_int), ("fix_pressure_points", ctypes.c_int)]
 
 
 class SolveOpts(ctypes.Structure):

@@ -13,7 +13,8 @@ OCEAN, LAND, PERIO = 0, 1, 3
 
 BASE = dict(xmin_deg=286.0, xmax_deg=350.0, ymin_deg=10.0, ymax_deg=74.0, periodic=0,
             hdim=4000.0, qz=1.0, alphaT=1.0e-4, alphaS=7.6e-4, ih=0, coriolis_on=1,
-            tres=1, sres=1, iza=2, ite=1, its=1, forcing_type=0, vmix=0, rho_mixing=0, tap=1)
+            tres=1, sres=1, iza=2, ite=1, its=1, forcing_type=0, vmix=0, rho_mixing=0, tap=1,
+            sint_sign=-1, intcon_i=-1, intcon_j=-1, fix_pressure_points=0)
 
 
 def gateway_16x16x16():
@@ -26,6 +27,21 @@ def gateway_16x16x16():
     return dict(BASE, n=16, m=16, l=16, xmin_deg=300.0, xmax_deg=340.0, ymin_deg=20.0, ymax_deg=60.0,
                 periodic=1, hdim=4000.0, qz=1.0, iza=2, ite=1, its=1, forcing_type=2, vmix=2, rho_mixing=0,
                 tap=1)
+
+
+def natl8_8x8x4():
+    """The reference's unit-test ocean (test/ocean/ocean_params.xml, driven by
+    src/tests/test_ocean.C): 8x8x4 cells, lon 286-350, lat 10-74, depth 4000 m,
+    the land mask data/mkmask/mask_natl8, fixed-partition vertical mixing
+    (Mixing = 1), T restoring, no S restoring (SRES = 0: the integral
+    condition on S), idealized forcing."""
+    return dict(BASE, n=8, m=8, l=4, periodic=0, vmix=1, rho_mixing=0, tap=1, tres=1, sres=0, iza=2, ite=1, its=1,
+                forcing_type=0)
+
+
+NATL8_STARTING_PARAMETERS = (("Combined Forcing", 0.0), ("Solar Forcing", 0.0), ("Salinity Forcing", 1.0),
+                             ("Wind Forcing", 1.0), ("Temperature Forcing", 10.0), ("SPL1", 2.0e3),
+                             ("SPL2", 0.01))
 
 
 # "Starting Parameters" of test/ocean/reft_ocean_params.xml

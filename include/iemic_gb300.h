@@ -62,6 +62,16 @@ typedef struct {
                                       IEMIC_ERR_ARG while either is nonzero with Mixing >= 1. */
     int rho_mixing;                /* "Rho Mixing" */
     int tap;                       /* "Taper" (tap of src/ocean/usr.F90; used by neutral physics only) */
+    int sint_sign;                 /* "Salinity Integral Sign" (-1 or 1; 0 is taken as -1). With sres = 0
+                                      the S row of cell (intcon_i, intcon_j, l-1) holds the integral
+                                      condition sint_sign * sum_cells cos(y_j) dfzT(k) S (THCM::intcond_S,
+                                      src/ocean/THCM.C:2180-2257): a dense row of the Jacobian over every S
+                                      unknown, F = sint_sign * (that sum), and the net salt flux of the
+                                      forcing is removed (qint, src/ocean/forcing.F90:121-160). */
+    int intcon_i, intcon_j;        /* "Integral row coordinate i/j" (0-based; -1: n-1, m-1); must be ocean */
+    int fix_pressure_points;       /* "Fix Pressure Points": the continuity rows of the surface pressures
+                                      (n-1, m-1) and (n-2, m-1) become identity rows, F = 0 there
+                                      (THCM::fixPressurePoints, THCM.C:2260-2297) */
 } iemic_config;
 
 typedef struct iemic_ocean iemic_ocean;

@@ -54,7 +54,8 @@ class Config(ctypes.Structure):
                 ("tres", ctypes.c_int), ("sres", ctypes.c_int),
                 ("iza", ctypes.c_int), ("ite", ctypes.c_int), ("its", ctypes.c_int),
                 ("forcing_type", ctypes.c_int), ("vmix", ctypes.c_int), ("rho_mixing", ctypes.c_int),
-                ("tap", ctypes.c_int)]
+                ("tap", ctypes.c_int), ("sint_sign", ctypes.c_int), ("intcon_i", ctypes.c_int),
+                ("intcon_j", ctypes.c_int), ("fix_pressure_points", ctypes.c_int)]
 
 
 class SolveOpts(ctypes.Structure):
@@ -129,6 +130,8 @@ class Oracle:
             self._landm_in = np.ascontiguousarray(landm, dtype=np.int32).ravel()
             lm = _ip(self._landm_in)
         self.h = self.L.oracle_create(ctypes.byref(c), lm)
+        if not self.h:
+            raise ValueError("oracle_create: the integral-condition row lies on land")
         self.n, self.m, self.l = cfg["n"], cfg["m"], cfg["l"]
         self.ndim = self.L.oracle_ndim(self.h)
 

@@ -52,6 +52,12 @@ struct Model {
     double xmin, xmax, ymin, ymax, hdim, qz, alphaT, alphaS;
     int ih, coriolis_on, TRES, SRES, iza, ite, its, forcing_type;
     int vmix = 0, rho_mixing = 0, tap = 1;   // "Mixing", "Rho Mixing", "Taper"
+    // SRES = 0: integral condition on S (THCM::intcond_S, src/ocean/THCM.C:2180-2257)
+    int sint_sign = -1, rowintcon = -1;      // 0-based row of the condition
+    double intCorrection = 0.0;              // THCM::setIntCondCorrection
+    std::vector<double> intcoef;             // cos(y_j) dfzT(k) at S of ocean cells (intcond_scaling)
+    // "Fix Pressure Points" (THCM::fixPressurePoints, THCM.C:2260-2297)
+    int rowPfix1 = -1, rowPfix2 = -1;
     const int coupled_T = 0, coupled_S = 0;
     // grid (src/ocean/grid.F90)
     double dx, dy, dz;
@@ -214,6 +220,19 @@ struct Model {
         return std::cos(PI * yy / ymax) + par[FPER] * yy / ymax;
     }
 
+    // ---- qint (src/ocean/forcing.F90:452-464) through thcm_forcing_integral
+    // (src/ocean/THCM.C:2653-2686): area mean of a surface field over ocean ----
+    double qint(std::vector<double>& f) {
+        double lfsint = 0.0, lsint = 0.0;
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int lmv = LM(i + 1, j + 1, l);
+                lfsint = f[size_t(i) + size_t(n) * j] * std::cos(Y(j + 1)) * double(1 - lmv) + lfsint;
+                lsint = std::cos(Y(j + 1)) * double(1 - lmv) + lsint;
+            }
+        return lfsint / lsint;
+    }
+
     // ---- forcing: src/ocean/forcing.F90:4-218 (uncoupled, restoring branches) ----
     void forcing() {
         std::fill(Frc.begin(), Frc.end(), 0.0);
@@ -235,7 +254,7 @@ struct Model {
         if (ite == 1 && coupled_T == 0) {
             for (int j = 1; j <= m; ++j)
                 for (int i = 1; i <= n; ++i) F2(tatm, i, j) = temfun(Y(j));
-            // TRES == 0 would call qint: restoring-only path here.
+            if (TRES == 0) temcor = qint(tatm);
         }
         for (int j = 1; j <= m; ++j)
             for (int i = 1; i <= n; ++i)
@@ -246,8 +265,13 @@ struct Model {
         if (its == 1) {
             for (int j = 1; j <= m; ++j)
                 for (int i = 1; i <= n; ++i) F2(emip, i, j) = salfun(Y(j)) * double(1 - LM(i, j, l));
+            if (SRES == 0) salcor = qint(emip);
         }
         double adapted_salcor = 0.0, spertcor = 0.0;
+        if (SRES == 0) {   // correct for a nonzero net flux
+            adapted_salcor = qint(adapted_emip);
+            spertcor = qint(spert);
+        }
         for (int j = 1; j <= m; ++j)
             for (int i = 1; i <= n; ++i)
                 Frc[find_row2(i, j, l, SS) - 1] =
@@ -1061,6 +1085,9 @@ struct Model {
                 coB[find_row2(i, j, k, TT) - 1] = -1.0;
                 coB[find_row2(i, j, k, SS) - 1] = -1.0;
             }
+        if (rowintcon >= 0) coB[rowintcon] = 0.0;   // assemble.F90:49; THCM.C:1233-1238
+        if (rowPfix1 >= 0) coB[rowPfix1] = 0.0;     // THCM.C:1220-1230
+        if (rowPfix2 >= 0) coB[rowPfix2] = 0.0;
     }
     // ---- matAvec: src/ocean/matetc.F90:147-166 ----
     void matAvec(const double* v1, double* v2) const {
@@ -1437,6 +1464,13 @@ struct Model {
                 F[row] = F[row] * double(1 - LM(i, j, k));
             }
         for (int r = 0; r < ndim; ++r) F[r] = -F[r];   // Epetra Scale(-1.0)
+        if (rowintcon >= 0) {   // THCM::evaluate (THCM.C:1014-1026): intSign (c . x - correction)
+            double dot = 0.0;
+            for (int q = 0; q < ndim; ++q) dot += intcoef[q] * un[q];
+            F[rowintcon] = sint_sign * (dot - intCorrection);
+        }
+        if (rowPfix1 >= 0) F[rowPfix1] = 0.0;   // THCM.C:1028-1041
+        if (rowPfix2 >= 0) F[rowPfix2] = 0.0;
     }
     void assemble_rhs_matrix(const double* un) {
         An = Al;
@@ -1510,6 +1544,11 @@ struct Model {
                 rows[g0 + 4 + q] = idx;
             }
         }
+        if (rowintcon >= 0) {   // CreateMaximalGraph(useSRES) with SRES = 0 (THCM.C:2542-2577)
+            auto& rr = rows[rowintcon];
+            rr.clear();
+            for (int k = 0; k < L; ++k) for (int j = 0; j < M; ++j) for (int i = 0; i < N; ++i) rr.push_back(fr(i, j, k, SS));
+        }
         for (int r = 0; r < ndim; ++r) {
             auto& rr = rows[r];
             std::sort(rr.begin(), rr.end());
@@ -1526,12 +1565,20 @@ struct Model {
         for (int r = 0; r < ndim; ++r) {
             const int* b = g_col.data() + g_ptr[r];
             const int* e = g_col.data() + g_ptr[r + 1];
+            if (r == rowintcon) {   // intcond_S replaces the row (THCM.C:1085, 2191-2230)
+                for (int q = g_ptr[r]; q < g_ptr[r + 1]; ++q) values[q] = sint_sign * intcoef[g_col[q]];
+                continue;
+            }
             for (int q = begA[r]; q < begA[r + 1]; ++q) {
                 int col = jcoA[q - 1] - 1;
                 const int* f = std::lower_bound(b, e, col);
                 if (f != e && *f == col) values[g_ptr[r] + (f - b)] = coA[q - 1];
                 else ++excluded;
             }
+        }
+        for (int r : {rowPfix1, rowPfix2}) {   // fixPressurePoints: identity rows
+            if (r < 0) continue;
+            for (int q = g_ptr[r]; q < g_ptr[r + 1]; ++q) values[q] = g_col[q] == r ? 1.0 : 0.0;
         }
         return excluded;
     }
@@ -1588,6 +1635,19 @@ struct Model {
         double dzne = dz * DFZT(l);
         QTnd = r0dim / (udim * cp0 * rhodim * hdim * dzne);
         QSnd = s0 * r0dim / (deltas * udim * hdim * dzne);
+        if (SRES == 0) {   // location of the integral condition (THCM.C:651-697)
+            const int Nic = c.intcon_i >= 0 ? c.intcon_i : n - 1, Mic = c.intcon_j >= 0 ? c.intcon_j : m - 1;
+            if (Nic >= n || Mic >= m || LM(Nic + 1, Mic + 1, l) != OCEAN) throw 1;
+            rowintcon = NUN * ((l - 1) * n * m + n * Mic + Nic) + SS - 1;
+            sint_sign = c.sint_sign == 0 ? -1 : c.sint_sign;
+            intcoef.assign(ndim, 0.0);   // intcond_scaling (thcm_utils.F90:285-312)
+            for (int k = 1; k <= l; ++k) for (int j = 1; j <= m; ++j) for (int i = 1; i <= n; ++i)
+                if (LM(i, j, k) == OCEAN) intcoef[find_row2(i, j, k, SS) - 1] = std::cos(Y(j)) * DFZT(k);
+        }
+        if (c.fix_pressure_points) {   // THCM.C:749-758
+            rowPfix1 = NUN * ((l - 1) * n * m + n * (m - 1) + (n - 1)) + PP - 1;
+            rowPfix2 = NUN * ((l - 1) * n * m + n * (m - 1) + (n - 2)) + PP - 1;
+        }
         stpnt();
         forcing();
         lin();
@@ -1602,7 +1662,12 @@ extern "C" {
 
 void* oracle_create(const iemic_oracle_config* cfg, const int* landm) {
     Model* M = new Model();
-    M->init(*cfg, landm);
+    try {
+        M->init(*cfg, landm);
+    } catch (...) {   // the integral-condition row is on land (THCM.C:671-690)
+        delete M;
+        return nullptr;
+    }
     return M;
 }
 void oracle_destroy(void* h) { delete static_cast<Model*>(h); }

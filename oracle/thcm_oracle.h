@@ -40,6 +40,9 @@ typedef struct {
     int vmix;                 // "Mixing" (vmix_GLB): 0 off, 1 fixed partition, 2 adaptive
     int rho_mixing;           // "Rho Mixing"
     int tap;                  // "Taper" (tap in usr.F90)
+    int sint_sign;            // "Salinity Integral Sign" (-1 or 1; 0 taken as -1)
+    int intcon_i, intcon_j;   // "Integral row coordinate i/j" (-1: n-1, m-1)
+    int fix_pressure_points;  // "Fix Pressure Points"
 } iemic_oracle_config;
 
 void* oracle_create(const iemic_oracle_config* cfg, const int* landm);

@@ -5,7 +5,8 @@
    a checkout of the reference), converted with the reader rules of readmask
    (src/ocean/topo.F90:41-60): per level k = 0..l+1 a header line, then rows
    j = m+1 down to 0 of n+2 digits (i = 0..n+1). Stored as int8 in the
-   (l+2, m+2, n+2) layout of the C ABI (i fastest).
+   (l+2, m+2, n+2) layout of the C ABI (i fastest). mask_natl8.npy: the 8x8x4
+   North-Atlantic mask of the reference's src/tests/test_ocean.C, the same way.
 2. oracle_box_seed0.npz / oracle_glob24_seed1.npz: values of the CPU oracle
    at seeded states -- F, J 1, J^T 1, every 97th value of J in the maximal
    graph and a SHA-256 of the graph's index arrays -- so that the oracle and
@@ -55,6 +56,9 @@ def main():
                                                                  "mask_global_96x38x12")
     if ref_mask is not None and os.path.exists(ref_mask):
         np.save(os.path.join(HERE, "mask_global_96x38x12.npy"), read_mask(ref_mask, 96, 38, 12))
+        # the mask of src/tests/test_ocean.C (test/ocean/ocean_params.xml: 8x8x4 North Atlantic)
+        np.save(os.path.join(HERE, "mask_natl8.npy"),
+                read_mask(os.path.join(args.reference, "data", "mkmask", "mask_natl8"), 8, 8, 4))
     for name, case, seed in (("box_seed0", box_case, 0), ("glob24_seed1", global_case, 1)):
         cfg, lm, frc = case()
         o = make_oracle(cfg, lm, frc)

@@ -20,6 +20,12 @@ def gateway_case(vmix=2):
     return cfg, g["landm"].astype(np.int32), None
 
 
+def natl8_case(sres=0, fix_pressure_points=0):
+    """The reference's src/tests/test_ocean.C ocean (mask_natl8, SRES = 0)."""
+    lm = np.load(os.path.join(GOLDEN, "mask_natl8.npy")).astype(np.int32)
+    return dict(W.natl8_8x8x4(), sres=sres, fix_pressure_points=fix_pressure_points), lm, None
+
+
 def gateway_golden():
     g = np.load(os.path.join(GOLDEN, "reft_ocean_reference.npz"))
     pars = dict(zip([str(s) for s in g["par_names"]], g["par_values"]))

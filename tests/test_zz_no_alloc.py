@@ -4,7 +4,9 @@ it must pass alone and after every other test in the process).
 Two calls in a row on the same handle, each compared bit for bit with the
 handle-scratch entry point, on the 16x16x4 box, a 24x12x6 periodic global
 ocean and the 16x16x16 gateway basin with vertical mixing (whose partition
-control also keeps its partial sums in the static array); calls on two
+control also keeps its partial sums in the static array) and the 8x8x4
+North-Atlantic basin with the integral condition on S and fixed pressure
+points; calls on two
 handles back to back, read on another stream right after each returns; a
 grid whose padded fields exceed the static scratch is rejected without
 touching the output.
@@ -14,7 +16,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from helpers import box_case, gateway_case, global_case, make_gpu, seeded_state
+from helpers import box_case, gateway_case, global_case, make_gpu, natl8_case, seeded_state
 
 pytestmark = pytest.mark.gpu
 
@@ -32,12 +34,17 @@ def _gateway():
     return gateway_case(2)
 
 
-@pytest.mark.parametrize("case", [box_case, global_case, _gateway])
+def _natl8():
+    return natl8_case(0, 1)
+
+
+@pytest.mark.parametrize("case", [box_case, global_case, _gateway, _natl8])
 def test_noalloc_rhs_matches_rhs_dev_twice(case):
     import torch
     from iemic import workloads as W
     cfg, lm, frc = case()
     g = make_gpu(cfg, lm, frc, W.GATEWAY_STARTING_PARAMETERS if cfg.get("vmix") else W.STARTING_PARAMETERS)
+    g.setPar("Combined Forcing", 0.5)
     L = g.L
     for seed in (0, 1):   # two calls in a row, different states
         x = _dev(seeded_state(cfg, seed, uvw=0.01))
