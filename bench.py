@@ -301,8 +301,7 @@ def cpu_continuation_sample(args, steps):
              "Wind Forcing": "WIND"}
     for name, v in W.STARTING_PARAMETERS:
         o.set_par(names[name], v)
-    o.set_par("COMB", 0.0)
-    fscale = float(np.linalg.norm(o.rhs(np.zeros(o.ndim))))
+    fscale = float(st0["fscale"])           # ||F(0)|| at the starting parameters, as the GPU arm uses
     o.set_par("COMB", float(st0["combined_forcing"]))
     par0 = float(st0["salinity_forcing"])
     o.set_par("SALT", par0)

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "engine.cuh"
@@ -789,6 +790,13 @@ static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const d
                       double* x, int m, int maxit, double tol, double* relres_out, int* iters_out) {
     Krylov& K = *e.kry;
     if (K.cyc_failed) return false;
+    // IEMIC_HOST_GMRES=1 steps the cycles from the host (the same iteration;
+    // for profilers that cannot see kernels inside conditional graph nodes)
+    static const bool host_only = [] {
+        const char* v = std::getenv("IEMIC_HOST_GMRES");
+        return v && *v && *v != '0';
+    }();
+    if (host_only) return false;
     if (!ensure_cycle_graph(e, lu, rp, ci, vals)) {
         K.cyc_failed = true;
         return false;

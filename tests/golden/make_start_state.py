@@ -38,8 +38,8 @@ def main():
         o.set_par({"Combined Forcing": "COMB", "Temperature Forcing": "TEMP", "Salinity Forcing": "SALT",
                    "Wind Forcing": "WIND"}[name], v)
     nd = o.ndim
+    fscale = float(np.linalg.norm(o.rhs(np.zeros(nd))))     # ||F(0)|| at the starting parameters
     o.set_par("COMB", 0.0)
-    fscale = float(np.linalg.norm(o.rhs(np.zeros(nd))))
     plan = Plan(o.landm(), cfg["n"], cfg["m"], cfg["l"], cfg["periodic"])
     M = MultifrontalModel(o, plan, policy="each")
     t0 = time.time()
