@@ -114,6 +114,7 @@ struct Engine {
     void spmv64(const double* x, double* y);
     void spmv32(const float* x, float* y);
     void free_solver();
+    void drop_factors();   // both factorisations and the Krylov workspace (keeps the plan)
     void ensure_solver();
     void build_preconditioner(int precision);
     int solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st);

@@ -443,12 +443,19 @@ void Engine::spmv32(const float* x, float* y) {
     ck(cudaGetLastError());
 }
 
-void Engine::free_solver() {
+void Engine::drop_factors() {
+    // the Krylov workspace goes too: its captured Arnoldi cycle holds the
+    // factorisation's buffers, and a new factorisation may reuse the address
     delete lu64;
     delete lu32;
     lu64 = lu32 = nullptr;
     free_krylov(kry);
     kry = nullptr;
+    fact64_stale = fact32_stale = true;
+}
+
+void Engine::free_solver() {
+    drop_factors();
     delete ndplan;
     ndplan = nullptr;
 }

@@ -1323,6 +1323,9 @@ struct WorkItem {
 // loads) and a tile's column groups are summed in shared memory
 constexpr int GR = 256, GC = 256, GT = 64, NCG = GR / GT, CGW = GC / NCG;
 enum { ST_LINV = 0, ST_UINV = 1, ST_L21 = 2, ST_U12 = 3, NSTAGE = 4 };
+// work-item stage codes of the product blocks L21 Linv11 and Uinv11 U12 (the
+// blocks and partial buffers of ST_L21 / ST_U12, read from the product store)
+enum { ST_P21 = 4, ST_Q12 = 5 };
 // rows and columns of a stage's block inside a front
 __host__ __device__ inline void stage_block(int st, int nf, int F, int& r0, int& r1, int& c0, int& c1) {
     r0 = st == ST_L21 ? nf : 0;
@@ -1390,6 +1393,9 @@ __device__ __forceinline__ void dd_acc(float& s, float& c, float a, float xh, fl
 // sg * sum_{c0 <= c < c1} A[c * ld] x[c - col0] with x staged in shared
 // memory (xs: FP64; xs2: its hi/lo FP32 split for FP32 factors). FP32
 // factors accumulate in compensated double-float, FP64 factors in FP64.
+// The factors are read-only while a sweep runs: loads take the
+// non-coherent path explicitly (kernels that also write, fence or use
+// atomics would otherwise get coherent loads).
 template <class T>
 __device__ __forceinline__ double row_dot(const T* __restrict__ A, int64_t ld, int c0, int c1, int col0,
                                           const double* xs, const float2* xs2, float sg) {
@@ -1440,6 +1446,7 @@ struct StageBufs {
 template <class T, int ST>
 __device__ __forceinline__ void gemv_stage(const WorkItem& it, const FrontDev& fr, const T* __restrict__ front,
                                            const double* __restrict__ X, const StageBufs& sb) {
+    // front: the factor store, or for ST_L21 / ST_U12 the product store
     double* __restrict__ part = sb.part[ST];
     const int64_t* __restrict__ part_off = sb.off[ST];
     const int F = fr.F, nf = fr.nf;
@@ -1569,14 +1576,17 @@ __global__ void __launch_bounds__(SDT) k_sub_diag(const FrontDev* __restrict__ f
 
 template <class T>
 __global__ void __launch_bounds__(GR) k_gemv_part(const FrontDev* __restrict__ fronts, const WorkItem* __restrict__ items,
-                                                  const T* __restrict__ front, const double* __restrict__ X, StageBufs sb) {
+                                                  const T* __restrict__ front, const T* __restrict__ prod,
+                                                  const double* __restrict__ X, StageBufs sb) {
     const WorkItem it = items[blockIdx.x];
     const FrontDev fr = fronts[it.front];
     switch (it.stage) {
         case ST_LINV: gemv_stage<T, ST_LINV>(it, fr, front, X, sb); break;
         case ST_UINV: gemv_stage<T, ST_UINV>(it, fr, front, X, sb); break;
         case ST_L21: gemv_stage<T, ST_L21>(it, fr, front, X, sb); break;
-        default: gemv_stage<T, ST_U12>(it, fr, front, X, sb); break;
+        case ST_U12: gemv_stage<T, ST_U12>(it, fr, front, X, sb); break;
+        case ST_P21: gemv_stage<T, ST_L21>(it, fr, prod, X, sb); break;
+        default: gemv_stage<T, ST_U12>(it, fr, prod, X, sb); break;
     }
 }
 
@@ -1614,6 +1624,27 @@ __global__ void k_stage_reduce(const FrontDev* __restrict__ fronts, const int* _
         WP[fr.woff + r] += s;
     } else {
         xred[fr.red0 + r] = s;
+    }
+}
+
+// Epilogues of the product sweeps, one thread per row of the front:
+//   forward  (F rows):  y = Linv11 P w_own -> W, WP;  u_B = w_B - (L21 Linv11) P w_own -> WP[B]
+//   backward (nf rows): x_own = Uinv11 y - (Uinv11 U12) x_B -> xred
+template <bool UP>
+__global__ void k_prod_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
+                              double* __restrict__ W, double* __restrict__ WP, double* __restrict__ xred) {
+    const int f = lf[blockIdx.y];
+    const FrontDev fr = fronts[f];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (UP) {
+        if (r >= fr.nf) return;
+        xred[fr.red0 + r] = stage_sum(ST_UINV, f, fr, r, sb) + stage_sum(ST_U12, f, fr, r, sb);
+    } else if (r < fr.nf) {
+        const double y = stage_sum(ST_LINV, f, fr, r, sb);
+        W[fr.woff + r] = y;
+        WP[fr.woff + r] = y;
+    } else if (r < fr.F) {
+        WP[fr.woff + r] += stage_sum(ST_L21, f, fr, r, sb);
     }
 }
 
@@ -1834,13 +1865,13 @@ int blocks_for(int64_t work, int per = NT) {
 // drivers
 // ===========================================================================
 NdLu::~NdLu() {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
         if (sweep_exec[k]) cudaGraphExecDestroy(sweep_exec[k]);
         if (sweep_exec_timed[k]) cudaGraphExecDestroy(sweep_exec_timed[k]);
     }
     if (factor_exec) cudaGraphExecDestroy(factor_exec);
     if (factor_exec_timed) cudaGraphExecDestroy(factor_exec_timed);
-    for (auto* t : {&factor_tmpl, &sweep_tmpl[0], &sweep_tmpl[1]})
+    for (auto* t : {&factor_tmpl, &sweep_tmpl[0], &sweep_tmpl[1], &sweep_tmpl[2]})
         for (const KTimer::Rec& r : *t) {
             cudaEventDestroy(r.a);
             cudaEventDestroy(r.b);
@@ -1989,6 +2020,38 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
         for (int g = 0; g < 4; ++g) lu.group_start[g].push_back(int(gitems[g].size()));
     }
     for (int g = 0; g < 4; ++g) lu.d_group_items[g] = upload(lu, gitems[g], s);
+    // product sweeps: per level one launch group per sweep, [0] Linv11 and
+    // L21 Linv11 (both read P w_own), [1] Uinv11 and Uinv11 U12 (read y and x_B)
+    {
+        const int mgroup_of[NSTAGE] = {0, 1, 0, 1};
+        const int mcode[NSTAGE] = {ST_LINV, ST_UINV, ST_P21, ST_Q12};
+        std::vector<WorkItem> mitems[2];
+        for (int g = 0; g < 2; ++g) {
+            lu.mgroup_start[g].assign(1, 0);
+            lu.mgroup_bytes[g].assign(plan.nlevels, 0.0);
+        }
+        for (int h = 0; h < plan.nlevels; ++h) {
+            for (int st = 0; st < NSTAGE; ++st) {
+                const int mg = mgroup_of[st];
+                for (int f : plan.level_fronts[h]) {
+                    const FrontDev& fr = plan.fronts[f];
+                    const double nf = fr.nf, nb = fr.nb;
+                    lu.mgroup_bytes[mg][h] += double(ts) * (st == ST_LINV ? nf * (nf - 1) / 2
+                                                            : st == ST_UINV ? nf * (nf + 1) / 2 : nf * nb);
+                    int r0, r1, c0, c1;
+                    stage_block(st, fr.nf, fr.F, r0, r1, c0, c1);
+                    for (int c = c0, ch = 0; c < c1; c += GC, ++ch)
+                        for (int r = r0; r < r1; r += GT) {
+                            if (st == ST_LINV && r + GT <= fr.nf && c >= r + GT) continue;
+                            if (st == ST_UINV && c + GC <= r) continue;
+                            mitems[mg].push_back(WorkItem{f, r, c, ch, mcode[st]});
+                        }
+                }
+            }
+            for (int g = 0; g < 2; ++g) lu.mgroup_start[g].push_back(int(mitems[g].size()));
+        }
+        for (int g = 0; g < 2; ++g) lu.d_mgroup_items[g] = upload(lu, mitems[g], s);
+    }
     // block substitution: per level and sub-step k, the fronts with more than
     // k super-blocks take super-block s = k (lower) or s = nsb - 1 - k (upper)
     {
@@ -2082,10 +2145,15 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
         std::vector<SplitGroup> groups;
         const int tile = prec ? FG_TM : 64;   // k_task_gemm_f32 / k_tri_gemm tile size
         int64_t tmax = 0, tmax2 = 0;
+        int maxnf = 0;
+        for (int h = 0; h < plan.nlevels; ++h) maxnf = std::max(maxnf, plan.level_maxnf[h]);
+        lu.subst = maxnf > subst_min_nf;
+        lu.products = !lu.subst;
         lu.tri_ranges.clear();
         lu.inv2_ranges.clear();
+        lu.prod_ranges.clear();
         for (int h = 0; h < plan.nlevels; ++h) {
-            std::vector<std::pair<int, int>> lv, lv2;
+            std::vector<std::pair<int, int>> lv, lv2, lv3;
             auto emit = [&](const TriTask& t) {
                 const int id = int(tasks.size());
                 tasks.push_back(t);
@@ -2189,18 +2257,36 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
                     if (int(groups.size()) > gb) lv2.push_back({-1 - gb, -1 - int(groups.size())});   // split-K reduce
                 }
             }
+            // (3) whole-inverse plans: the products of the solve sweeps, into
+            //     the product store (the tasks' scratch) at the offsets of the
+            //     blocks they replace:  L21 Linv11 (nb x nf)  and  Uinv11 U12 (nf x nb)
+            if (lu.products) {
+                const int tb = int(tiles.size());
+                for (int f : plan.level_fronts[h]) {
+                    const FrontDev& fr = plan.fronts[f];
+                    const int nf = fr.nf, nb = fr.nb, F = fr.F;
+                    if (nf == 0 || nb == 0) continue;
+                    const int64_t l21 = fr.foff + nf, u12 = fr.foff + int64_t(F) * nf;
+                    emit(TriTask{l21, fr.foff, l21, F, F, F, nb, nf, nf, OP_DENSE, OP_LOWER_UNIT, 0, 0, 1, 1.f});
+                    emit(TriTask{fr.foff, u12, u12, F, nf, nf, nf, nb, nf, OP_UPPER, OP_DENSE, 0, 0, 1, 1.f});
+                }
+                if (int(tiles.size()) > tb) lv3.push_back({tb, int(tiles.size())});
+            }
             lu.tri_ranges.push_back(lv);
             lu.inv2_ranges.push_back(lv2);
+            lu.prod_ranges.push_back(lv3);
         }
         lu.d_tri_tasks = upload(lu, tasks, s);
         lu.d_tri_tiles = upload(lu, tiles, s);
         lu.d_tri_groups = upload(lu, groups, s);
         lu.d_tri_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax, 1)));
         lu.inv2_scratch_entries = tmax2;
-        int maxnf = 0;
-        for (int h = 0; h < plan.nlevels; ++h) maxnf = std::max(maxnf, plan.level_maxnf[h]);
-        lu.subst = maxnf > subst_min_nf;
         if (!lu.subst) lu.d_inv2_scratch = dmalloc(lu, ts * size_t(std::max<int64_t>(tmax2, 1)));
+        if (lu.products) {
+            const size_t pb = ts * size_t(std::max<int64_t>(plan.factor_entries, 1));
+            lu.d_prod = dmalloc(lu, pb);
+            ck(cudaMemsetAsync(lu.d_prod, 0, pb, s));
+        }
         ck(cudaStreamCreateWithFlags(&lu.side, cudaStreamNonBlocking));
         lu.fork_ev.assign(plan.nlevels, nullptr);
         for (auto& e : lu.fork_ev) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -2398,6 +2484,8 @@ static void factor_body(NdLu& lu, const int* rp, const int* ci, const double* va
         if (!lu.subst)
             for (const auto& rg : lu.inv2_ranges[h])
                 tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_inv2_scratch), lu.side);
+        if (lu.products)
+            for (const auto& rg : lu.prod_ranges[h]) tri_range<T>(lu, rg, factor, static_cast<T*>(lu.d_prod), lu.side);
         if (ev_inv) lu.timer->stop(ev_inv, lu.side, IEMIC_KC_FACTOR_INVERSE, 0.0, 0.0);
     }
     // the factorisation ends when the side stream's inverses are done
@@ -2526,8 +2614,34 @@ static void launch_group(NdLu& lu, int g, int h, const T* front, double* WP, cud
     if (!ni) return;
     cudaEvent_t ev = lu.timer ? lu.timer->start(s) : nullptr;
     k_gemv_part<T><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_group_items[g]) +
-                                         lu.group_start[g][h], front, WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
+                                         lu.group_start[g][h], front, front, WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
     if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.group_bytes[g][h], 2.0 * lu.group_bytes[g][h] / sizeof(T));
+}
+// one GEMV launch of the product sweeps (g = 0 forward, 1 backward) over
+// level h, both stages of the level, and its epilogue
+template <class T>
+static void launch_mgroup(NdLu& lu, int g, int h, double* W, double* WP, double* red, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    KTimer* kt = lu.timer;
+    const int ni = lu.mgroup_start[g][h + 1] - lu.mgroup_start[g][h];
+    if (ni > 0) {
+        cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+        k_gemv_part<T><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_mgroup_items[g]) +
+                                             lu.mgroup_start[g][h], static_cast<const T*>(lu.d_factor),
+                                         static_cast<const T*>(lu.d_prod), WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
+        if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.mgroup_bytes[g][h], 2.0 * lu.mgroup_bytes[g][h] / sizeof(T));
+    }
+    const int nfr = lu.level_start[h + 1] - lu.level_start[h];
+    const int* lf = lu.d_level_fronts + lu.level_start[h];
+    const int rows = g == 0 ? P.level_maxF[h] : P.level_maxnf[h];
+    if (rows <= 0) return;
+    cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+    if (g == 0)
+        k_prod_reduce<false><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red);
+    else
+        k_prod_reduce<true><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red);
+    IEMIC_COUNT_LAUNCH();
+    if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
 }
 template <int ST>
 static void launch_reduce(NdLu& lu, int h, double* W, double* WP, double* red, cudaStream_t s) {
@@ -2564,11 +2678,16 @@ static void sub_steps(NdLu& lu, int h, const T* factor, double* W, double* WP, d
 }
 
 // The forward and backward sweeps over the levels: internal buffers only
-// (red -> red), so they can be captured once into a CUDA graph. The
-// triangles L11 / U11 are applied by block substitution (full = false) or,
-// once their whole inverses exist (after a transposed solve), as GEMVs.
+// (red -> red), so they can be captured once into a CUDA graph. Modes:
+// 0: L11 / U11 applied by block substitution (plans with large fronts);
+// 1: their whole inverses as GEMVs (such a plan after a transposed solve);
+// 2: whole inverses and the product store: per level and sweep one GEMV
+//    launch, whose two stages read the same gathered vector, and one epilogue
+//      forward:  [y ; u_B] = [Linv11 ; -(L21 Linv11)] P w_own  (+ [0 ; w_B])
+//      backward: x_own = Uinv11 y - (Uinv11 U12) x_B
 template <class T, int B>
-static void sweeps_t(NdLu& lu, bool full, cudaStream_t s) {
+static void sweeps_t(NdLu& lu, int mode, cudaStream_t s) {
+    const bool full = mode >= 1, prod = mode == 2;
     const NdPlan& P = *lu.plan;
     double* red = static_cast<double*>(lu.d_red);
     double* W = static_cast<double*>(lu.d_w);
@@ -2583,6 +2702,10 @@ static void sweeps_t(NdLu& lu, bool full, cudaStream_t s) {
             k_fwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of,
                                                                                 lu.d_einv, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
+        if (prod) {   // both stages in one launch, one epilogue
+            launch_mgroup<T>(lu, 0, h, W, WP, red, s);
+            continue;
         }
         if (full) {
             launch_group<T>(lu, 0, h, front, WP, s);
@@ -2600,6 +2723,10 @@ static void sweeps_t(NdLu& lu, bool full, cudaStream_t s) {
             cudaEvent_t ev = kt ? kt->start(s) : nullptr;
             k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
+        }
+        if (prod) {   // both stages in one launch, one epilogue
+            launch_mgroup<T>(lu, 1, h, W, WP, red, s);
+            continue;
         }
         launch_group<T>(lu, 2, h, front, WP, s);
         launch_reduce<ST_U12>(lu, h, W, WP, red, s);
@@ -2623,20 +2750,20 @@ static void apply_t(NdLu& lu, const int* rp, const int* ci, const double* val, c
                                                             lu.d_dr, r, red); IEMIC_COUNT_LAUNCH();
         if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
     }
-    const int fm = lu.full_inverse ? 1 : 0;
+    const int fm = lu.products ? 2 : lu.full_inverse ? 1 : 0;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     ck(cudaStreamIsCapturing(s, &cap));
     if (cap == cudaStreamCaptureStatusActive) {
         // captured into the caller's graph (the device-driven GMRES cycle):
         // the sweep kernels themselves, not a launch of the sweep graph
-        sweeps_t<T, B>(lu, fm == 1, s);
+        sweeps_t<T, B>(lu, fm, s);
     } else if (kt && kt->on) {
         timed_graph(lu, lu.sweep_exec_timed[fm], lu.sweep_tmpl[fm], lu.sweep_launches_timed[fm], s,
-                    [&] { sweeps_t<T, B>(lu, fm == 1, s); });
+                    [&] { sweeps_t<T, B>(lu, fm, s); });
     } else {
         if (!lu.sweep_exec[fm]) {
             const long long n0 = launch_counter();
-            cudaGraph_t g = capture_graph(s, [&] { sweeps_t<T, B>(lu, fm == 1, s); });
+            cudaGraph_t g = capture_graph(s, [&] { sweeps_t<T, B>(lu, fm, s); });
             lu.sweep_launches[fm] = launch_counter() - n0;
             launch_counter() = n0;
             const cudaError_t e = cudaGraphInstantiate(&lu.sweep_exec[fm], g, 0);

@@ -124,17 +124,30 @@ struct NdLu {
     std::vector<cudaEvent_t> fork_ev;       // per level
     cudaEvent_t join_ev = nullptr;
     bool full_inverse = false;              // L11 / U11 replaced by their whole inverses
+    // whole-inverse plans: the products L21 Linv11 and Uinv11 U12 in a store
+    // laid out like the factor store (the same offsets; the nf x nf squares
+    // unused), computed with the inverses. The two GEMV stages of a level and
+    // sweep then read the same gathered vector and run as one launch with one
+    // epilogue (product sweeps)
+    void* d_prod = nullptr;
+    bool products = false;
+    std::vector<std::vector<std::pair<int, int>>> prod_ranges;   // product tasks per level
+    void* d_mgroup_items[2] = {nullptr, nullptr};   // [0] Linv11 + L21 Linv11, [1] Uinv11 + Uinv11 U12
+    std::vector<int> mgroup_start[2];               // per level offsets
+    std::vector<double> mgroup_bytes[2];            // per level: factor bytes the launch reads
     double tri_flops = 0.0;
     cudaGraphExec_t factor_exec = nullptr;  // captured factorisation
-    // captured forward + backward level sweeps, [0] block substitution, [1] whole inverses
-    cudaGraphExec_t sweep_exec[2] = {nullptr, nullptr};
+    // captured forward + backward level sweeps, [0] block substitution,
+    // [1] whole inverses, [2] whole inverses with the products (one GEMV
+    // launch per level and sweep)
+    cudaGraphExec_t sweep_exec[3] = {nullptr, nullptr, nullptr};
     // the same graphs with timing event nodes (kernel timing on)
-    cudaGraphExec_t factor_exec_timed = nullptr, sweep_exec_timed[2] = {nullptr, nullptr};
-    std::vector<KTimer::Rec> factor_tmpl, sweep_tmpl[2];
-    long long factor_launches_timed = 0, sweep_launches_timed[2] = {0, 0};
+    cudaGraphExec_t factor_exec_timed = nullptr, sweep_exec_timed[3] = {nullptr, nullptr, nullptr};
+    std::vector<KTimer::Rec> factor_tmpl, sweep_tmpl[3];
+    long long factor_launches_timed = 0, sweep_launches_timed[3] = {0, 0, 0};
     long long factor_launches = 0;
     const void *fg_rp = nullptr, *fg_ci = nullptr, *fg_val = nullptr;   // arrays the factor graph reads
-    long long sweep_launches[2] = {0, 0};   // kernels in the captured sweeps
+    long long sweep_launches[3] = {0, 0, 0};   // kernels in the captured sweeps
     int npert = 0;
     int nnan = 0;
     bool factored = false;

@@ -129,11 +129,8 @@ int iemic_set_substitution_threshold(iemic_ocean* h, int max_inverse_nf) {
     GUARD_BEGIN
     if (max_inverse_nf != h->e.subst_min_nf) {
         ck(cudaStreamSynchronize(h->e.stream));
-        delete h->e.lu64;
-        delete h->e.lu32;
-        h->e.lu64 = h->e.lu32 = nullptr;
+        h->e.drop_factors();
         h->e.subst_min_nf = max_inverse_nf;
-        h->e.fact64_stale = h->e.fact32_stale = true;
     }
     GUARD_END
 }
