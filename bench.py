@@ -348,6 +348,8 @@ def run_reference(args, rank, world):
             "data": "synthetic (seeded land mask, idealized forcing)",
             "config": workload_config(args, d["cfg"], d["nd"], d["par0"], d["fscale"]),
             "impl": "reference", "cpu_baseline": base, "newton_iters": st["newton_iters"],
+            "arm_preconditioner_policy": "FP64 multifrontal LU rebuilt once per continuation step (Ocean::preProcess), "
+                                         "GMRES(100) on it for the step's later Jacobians",
             "continuation": {"steps": st["steps"], "failed_steps": st["failed_steps"], "par": d["par"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

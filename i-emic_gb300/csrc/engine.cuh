@@ -67,7 +67,6 @@ struct Engine {
     long fact_gen[2] = {0, 0}, wt_gen[2] = {-1, -1};
     int *d_rowptr = nullptr, *d_col = nullptr;
     double* d_val = nullptr;
-    float* d_val32 = nullptr;
 
     bool jac_valid = false;
     bool fact64_stale = true, fact32_stale = true;   // J changed since the last factorisation
@@ -112,7 +111,6 @@ struct Engine {
 
     // linear algebra (krylov.cu)
     void spmv64(const double* x, double* y);
-    void spmv32(const float* x, float* y);
     void free_solver();
     void drop_factors();   // both factorisations and the Krylov workspace (keeps the plan)
     void ensure_solver();

@@ -15,10 +15,10 @@
 // stored in FP32 (half the bytes, FP32 GEMM rate); its triangular solves
 // accumulate in FP64 and GMRES, J and the convergence test are FP64. This is
 // GMRES-based iterative refinement with a low-precision factorisation
-// (Carson & Higham, SIAM J. Sci. Comput. 40 (2018) A817). The all-FP32 inner
-// Krylov variant (IEMIC_PREC_FP32_KRYLOV: J, basis and inner products in FP32,
-// FP64 residual refinement outside) stalls on the 96x38x12 ocean, whose
-// Jacobian has a condition number near 1e8, and is kept as an option only.
+// (Carson & Higham, SIAM J. Sci. Comput. 40 (2018) A817). An all-FP32 inner
+// Krylov solve (J, basis and inner products in FP32 inside FP64 residual
+// refinement) stalled on the 96x38x12 ocean, whose Jacobian has a condition
+// number near 1e8, and is not offered.
 //
 // SpMV: rows hold 7..24 entries, so four lanes share a row and reduce with
 // warp shuffles; a warp covers eight consecutive rows (contiguous loads of
@@ -385,10 +385,6 @@ void launch_spmv64(int nrows, const int* rp, const int* ci, const double* v, con
                    cudaStream_t s) {
     spmv_launch<double>(nrows, rp, ci, v, x, y, skip, s);
 }
-void launch_spmv32(int nrows, const int* rp, const int* ci, const float* v, const float* x, float* y, int skip,
-                   cudaStream_t s) {
-    spmv_launch<float>(nrows, rp, ci, v, x, y, skip, s);
-}
 
 // Krylov workspace (both precisions share the layout)
 struct Krylov {
@@ -436,10 +432,6 @@ static void free_krylov(Krylov* k) {
 
 void Engine::spmv64(const double* x, double* y) {
     launch_spmv64(ndim, d_rowptr, d_col, d_val, x, y, rowintcon, stream);
-    ck(cudaGetLastError());
-}
-void Engine::spmv32(const float* x, float* y) {
-    launch_spmv32(ndim, d_rowptr, d_col, d_val32, x, y, rowintcon, stream);
     ck(cudaGetLastError());
 }
 
@@ -866,9 +858,7 @@ static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const d
 int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
     if (!jac_valid) return IEMIC_ERR_STATE;
     if (o.transpose) return solve_transpose_dev(b, x, o, st);
-    // IEMIC_PREC_MIXED: FP32 factors under an FP64 Krylov solve;
-    // IEMIC_PREC_FP32_KRYLOV: FP32 factors and FP32 GMRES inside FP64 refinement
-    const bool fp32_krylov = o.precision == IEMIC_PREC_FP32_KRYLOV;
+    // IEMIC_PREC_MIXED: FP32 factors under an FP64 Krylov solve
     const int prec = o.precision == IEMIC_PREC_FP64 ? IEMIC_PREC_FP64 : IEMIC_PREC_MIXED;
     auto t0 = std::chrono::steady_clock::now();
     ensure_solver();
@@ -881,7 +871,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     st.perturbed_pivots = lu->npert;
     auto t1 = std::chrono::steady_clock::now();
     st.time_factor_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
-    ensure_krylov(*this, o.restart, fp32_krylov ? 1 : 0);
+    ensure_krylov(*this, o.restart, 0);
     Krylov& K = *kry;
     const int n = ndim;
     const int G = vgrid(n);
@@ -900,52 +890,23 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
         return IEMIC_OK;
     }
     int rc = IEMIC_OK;
-    double relres = 1.0;
-    if (!fp32_krylov) {
-        scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
-        double est = 1.0;
-        int its = 0;
-        if (!timer.on && gmres_dev(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
-                                   &est, &its))
-            st.iters += its;
-        else
-            st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
-                                      &est, false, rowintcon);
-        axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
-        residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
-        multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
-        double rn2 = 0.0;
-        ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
-        ck(cudaStreamSynchronize(s));
-        relres = std::sqrt(rn2) / bnorm;
-    } else {
-        // FP64 iterative refinement around FP32 GMRES
-        float* r32 = static_cast<float*>(K.rhsT);
-        float* d32 = static_cast<float*>(K.xT);
-        ck(cudaMemcpyAsync(K.r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        double rnorm = bnorm;
-        for (int ref = 0;; ++ref) {
-            relres = rnorm / bnorm;
-            if (!std::isfinite(relres)) return IEMIC_ERR_NAN;
-            if (relres <= o.tol) break;
-            if (ref >= o.max_refinements || st.iters >= o.max_iters) break;
-            convert<double, float><<<G, 256, 0, s>>>(n, K.r64, r32, 1.0 / rnorm); IEMIC_COUNT_LAUNCH();
-            double est = 1.0;
-            double inner = std::max(o.inner_tol, 0.5 * o.tol / relres);
-            st.iters += gmres<float>(*this, *lu, d_rowptr, d_col, d_val32, r32, d32, o.restart, o.max_iters - st.iters, inner,
-                                     &est, false, rowintcon);
-            axpy_into<float><<<G, 256, 0, s>>>(n, rnorm, d32, x); IEMIC_COUNT_LAUNCH();
-            residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
-            multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
-            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
-            double rn2 = 0.0;
-            ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
-            ck(cudaStreamSynchronize(s));
-            rnorm = std::sqrt(rn2);
-            st.refinements += 1;
-        }
-    }
+    scale_by<double><<<G, 256, 0, s>>>(n, b, 1.0 / bnorm, K.r64); IEMIC_COUNT_LAUNCH();
+    double est = 1.0;
+    int its = 0;
+    if (!timer.on && gmres_dev(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
+                               &est, &its))
+        st.iters += its;
+    else
+        st.iters += gmres<double>(*this, *lu, d_rowptr, d_col, d_val, K.r64, K.x64, o.restart, o.max_iters, o.tol,
+                                  &est, false, rowintcon);
+    axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
+    residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
+    multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    double rn2 = 0.0;
+    ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    const double relres = std::sqrt(rn2) / bnorm;
     st.relres = relres;
     timer.drain();
     auto t2 = std::chrono::steady_clock::now();
@@ -995,7 +956,6 @@ void Engine::ensure_transpose() {
 // from the same factorisation as the forward solve (FP64 or FP32 factors).
 int Engine::solve_transpose_dev(const double* b, double* x, const iemic_solve_opts& o, iemic_solve_stats& st) {
     if (!jac_valid) return IEMIC_ERR_STATE;
-    if (o.precision == IEMIC_PREC_FP32_KRYLOV) return IEMIC_ERR_ARG;
     const int prec = o.precision == IEMIC_PREC_FP64 ? IEMIC_PREC_FP64 : IEMIC_PREC_MIXED;
     auto t0 = std::chrono::steady_clock::now();
     ensure_solver();

@@ -348,7 +348,6 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
     d_col = static_cast<int*>(dalloc(sizeof(int) * size_t(nnz)));
     d_slot = static_cast<int8_t*>(dalloc(slot.size()));
     d_val = static_cast<double*>(dalloc(sizeof(double) * size_t(nnz)));
-    d_val32 = static_cast<float*>(dalloc(sizeof(float) * size_t(nnz)));
     ck(cudaMemcpyAsync(d_rowptr, row_ptr.data(), sizeof(int) * row_ptr.size(), cudaMemcpyHostToDevice, stream));
     ck(cudaMemcpyAsync(d_slot, slot.data(), slot.size(), cudaMemcpyHostToDevice, stream));
     pat.row_ptr = d_rowptr; pat.col_idx = d_col; pat.slot = d_slot;
@@ -366,7 +365,6 @@ void Engine::init(const iemic_config& c, const int* lm_in) {
     }
     ck(cudaGetLastError());
     ck(cudaMemsetAsync(d_val, 0, sizeof(double) * size_t(nnz), stream));
-    ck(cudaMemsetAsync(d_val32, 0, sizeof(float) * size_t(nnz), stream));
     update_forcing();
     lin();
     launch_mass(geo, P, d_B, stream);
@@ -445,10 +443,10 @@ void Engine::jacobian_dev(const double* x) {
     cudaEvent_t ev = timer.start(stream);
     launch_usol(geo, x, d_pads, stream);
     mix_control(x, d_mixpart);
-    launch_jacobian(geo, P, mp, pat, d_al, d_pads, d_val, d_val32, stream);
-    launch_special_jac(int(nc), d_rowptr, d_col, d_intcoef, d_val, d_val32, rowintcon, sint_sign, rowPfix1, rowPfix2,
+    launch_jacobian(geo, P, mp, pat, d_al, d_pads, d_val, nullptr, stream);
+    launch_special_jac(int(nc), d_rowptr, d_col, d_intcoef, d_val, nullptr, rowintcon, sint_sign, rowPfix1, rowPfix2,
                        stream);
-    timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 12.0 * double(nnz) + 8.0 * 3.0 * ndim, 0.0);
+    timer.stop(ev, stream, IEMIC_KC_ASSEMBLY, 8.0 * double(nnz) + 8.0 * 3.0 * ndim, 0.0);
     ck(cudaGetLastError());
     jac_valid = true;
     fact64_stale = fact32_stale = true;

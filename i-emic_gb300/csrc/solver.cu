@@ -30,8 +30,6 @@ void iemic_default_solve_opts(iemic_solve_opts* o) {
     o->restart = 100;          // Belos "Num Blocks" (FGMRES iterations)
     o->max_iters = 1000;
     o->tol = 1e-8;
-    o->max_refinements = 20;
-    o->inner_tol = 1e-4;
     o->transpose = 0;
     o->reuse_preconditioner = 0;
 }
@@ -74,7 +72,7 @@ int iemic_solve_dev(iemic_ocean* h, const double* b, double* x, const iemic_solv
     iemic_default_solve_opts(&oo);
     if (o) oo = *o;
     if (oo.restart < 1 || oo.restart > 1000 || oo.max_iters < 1 || !(oo.tol > 0)) return IEMIC_ERR_ARG;
-    if (oo.precision < 0 || oo.precision > 2) return IEMIC_ERR_ARG;
+    if (oo.precision < 0 || oo.precision > 1) return IEMIC_ERR_ARG;
     iemic_solve_stats s{};
     int rc;
     try {

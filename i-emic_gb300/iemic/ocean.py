@@ -28,7 +28,7 @@ PARAMETER_NAMES = {
 ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "not converged", -4: "NaN/Inf",
           -5: "zero pivot", -6: "call order", -7: "device allocation failed"}
 
-PREC_FP64, PREC_MIXED, PREC_FP32_KRYLOV = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
 
 
 class IemicError(RuntimeError):
@@ -53,14 +53,13 @@ class Config(ctypes.Structure):
 
 class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("restart", ctypes.c_int), ("max_iters", ctypes.c_int),
-                ("tol", ctypes.c_double), ("max_refinements", ctypes.c_int),
-                ("inner_tol", ctypes.c_double), ("transpose", ctypes.c_int),
+                ("tol", ctypes.c_double), ("transpose", ctypes.c_int),
                 ("reuse_preconditioner", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int), ("factorizations", ctypes.c_int), ("perturbed_pivots", ctypes.c_int),
-                ("refinements", ctypes.c_int), ("relres", ctypes.c_double),
+                ("relres", ctypes.c_double),
                 ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
 
 
@@ -404,7 +403,7 @@ class Ocean:
         x = np.zeros(self.ndim)
         st = SolveStats()
         rc = self.L.iemic_solve(self._h, _dp(b), _dp(x), ctypes.byref(o), ctypes.byref(st))
-        stats = dict(iters=st.iters, refinements=st.refinements, relres=st.relres,
+        stats = dict(iters=st.iters, relres=st.relres,
                      factorizations=st.factorizations, perturbed_pivots=st.perturbed_pivots,
                      time_factor_ms=st.time_factor_ms, time_solve_ms=st.time_solve_ms, status=rc)
         if rc not in (0, -3):

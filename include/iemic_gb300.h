@@ -125,17 +125,13 @@ int iemic_mass(iemic_ocean* h, double* diagB);
 int iemic_apply_matrix(iemic_ocean* h, const double* v, double* out);
 
 /* Linear solve options / statistics (Ocean::solve, Ocean.C:1070-1147). */
-enum { IEMIC_PREC_FP64 = 0, IEMIC_PREC_MIXED = 1, IEMIC_PREC_FP32_KRYLOV = 2 };
+enum { IEMIC_PREC_FP64 = 0, IEMIC_PREC_MIXED = 1 };
 typedef struct {
     int precision;         /* IEMIC_PREC_FP64: FP64 GMRES + FP64 factors;
-                              IEMIC_PREC_MIXED: FP64 GMRES + FP32 factors (FP64-accumulated solves);
-                              IEMIC_PREC_FP32_KRYLOV: FP32 GMRES + FP32 factors inside FP64
-                              residual refinement (experimental) */
+                              IEMIC_PREC_MIXED: FP64 GMRES + FP32 factors (compensated solves) */
     int restart;           /* GMRES restart length ("FGMRES iterations") */
     int max_iters;         /* cap on total inner iterations */
     double tol;            /* relative residual target ||b - J x|| / ||b|| */
-    int max_refinements;   /* outer FP64 refinement steps (FP32_KRYLOV only) */
-    double inner_tol;      /* FP32 inner relative tolerance (FP32_KRYLOV only) */
     int transpose;         /* 0: J x = b, 1: J^T x = b (adjoint solve) */
     int reuse_preconditioner; /* 0: refactor when J changed since the last factorisation;
                                  1: keep the existing factorisation (the reference recomputes its
@@ -145,7 +141,6 @@ typedef struct {
     int iters;             /* total inner Krylov iterations */
     int factorizations;    /* preconditioner (re)builds performed by this call */
     int perturbed_pivots;  /* pivots the last factorisation had to perturb */
-    int refinements;       /* outer refinement steps */
     double relres;         /* final FP64 ||b - J x|| / ||b|| */
     double time_factor_ms; /* time spent (re)building the preconditioner */
     double time_solve_ms;  /* time spent in the Krylov solve */
