@@ -70,7 +70,13 @@ struct DevVecs {
 //     rent-or-buy); once it exceeds it, the next solve refactors the current
 //     Jacobian. The same budget caps a solve that runs on the factors of an
 //     older Jacobian: when it is spent before the solve converges, the solve
-//     is repeated on a fresh factorisation of the current Jacobian.
+//     is repeated on a fresh factorisation of the current Jacobian. After
+//     such a failure, the later Jacobians of the same continuation step are
+//     factorised directly when fresh factors themselves need at least 8
+//     iterations: inexact (FP32) factors have little margin, and near a fold,
+//     where the Jacobian moves fast, the next attempts on old factors fail as
+//     well. Exact (FP64) factors, a few iterations when fresh and expensive to
+//     rebuild, keep the budget rule.
 struct ModelOps {
     Engine& e;
     iemic_solve_opts solve_opts;
@@ -82,6 +88,7 @@ struct ModelOps {
     double fact_ms = 0.0, excess_ms = 0.0;   // cost of the current factorisation, Krylov time beyond its first solve
     int base_iters = 0;                      // iterations of the first solve on the current factorisation
     double iter_ms = 0.0;                    // time of one Krylov iteration, from the last solve
+    bool stale_failed = false;               // a solve on older factors failed in this step
     bool trace = false;
 
     ModelOps(Engine& en, const iemic_solve_opts& o, int pol) : e(en), solve_opts(o), policy(pol) {
@@ -101,7 +108,10 @@ struct ModelOps {
         t_asm += ms_since(t);
         ++jac_gen;
     }
-    void pre_process() { recompute = true; }
+    void pre_process() {
+        recompute = true;
+        stale_failed = false;
+    }
     int solve_once(const double* b, double* x, bool refactor, int cap) {
         iemic_solve_opts o = solve_opts;
         o.reuse_preconditioner = refactor ? 0 : 1;
@@ -134,7 +144,8 @@ struct ModelOps {
     }
     void solve(const double* b, double* x) {
         const bool newer = fact_gen != jac_gen;
-        const bool need = recompute || (policy == 1 && newer) || (policy == 2 && newer && excess_ms >= fact_ms);
+        const bool need = recompute || (policy == 1 && newer) ||
+                          (policy == 2 && newer && (excess_ms >= fact_ms || (stale_failed && base_iters >= 8)));
         const bool stale = policy == 2 && !need && newer;
         int cap = 0;
         if (stale && iter_ms > 0.0)   // iterations the remaining rebuild budget pays for
@@ -142,6 +153,7 @@ struct ModelOps {
         int rc = solve_once(b, x, need, cap);
         if (rc == IEMIC_ERR_NOT_CONVERGED && stale) {
             ++retries;
+            stale_failed = true;
             rc = solve_once(b, x, true, 0);
         }
         if (rc == IEMIC_ERR_NOT_CONVERGED) ++unconverged;

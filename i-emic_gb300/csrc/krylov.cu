@@ -155,12 +155,29 @@ __global__ void __launch_bounds__(256) multidot(int n, int nv, const T* __restri
         __syncthreads();
     }
 }
-// dots[i] = sum over blocks of the partials; also accumulates into h if given
-__global__ void reduce_parts(int nblocks, int nv, const double* __restrict__ part, double* __restrict__ dots,
-                             double* __restrict__ hacc, int first) {
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-        double s = 0.0;
-        for (int b = 0; b < nblocks; ++b) s += part[size_t(b) * nv + i];
+// The sum of the nblocks partials of dot product i (part[b * ldp + i]) by one
+// block of RT threads: strided per-thread sums, then a fixed-order tree in
+// shared memory, so the result is deterministic. Every thread returns it.
+constexpr int RT = 256;
+__device__ __forceinline__ double sum_parts(int nblocks, int ldp, int i, const double* __restrict__ part) {
+    __shared__ double red[RT];
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += RT) s += part[size_t(b) * ldp + i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = RT / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    return red[0];
+}
+// dots[i] = sum over blocks of the partials, one CTA per dot product (grid nv,
+// RT threads); also accumulates into h if given
+__global__ void __launch_bounds__(RT) reduce_parts(int nblocks, int nv, const double* __restrict__ part,
+                                                   double* __restrict__ dots, double* __restrict__ hacc, int first) {
+    const int i = blockIdx.x;
+    const double s = sum_parts(nblocks, nv, i, part);
+    if (threadIdx.x == 0) {
         dots[i] = s;
         if (hacc) hacc[i] = first ? s : hacc[i] + s;
     }
@@ -263,14 +280,17 @@ __global__ void __launch_bounds__(256) multidot_ctl(int n, const KryCtl* __restr
         __syncthreads();
     }
 }
-// dots = sum of the partials; column j of H gets them (first pass) or adds them
-__global__ void reduce_parts_ctl(int nblocks, int ldp, const KryCtl* __restrict__ ctl, const double* __restrict__ part,
-                                 double* __restrict__ dots, double* __restrict__ H, int first) {
-    const int nv = ctl->j + 1;
-    double* col = H + size_t(ctl->m + 1) * ctl->j;
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-        double sum = 0.0;
-        for (int b = 0; b < nblocks; ++b) sum += part[size_t(b) * ldp + i];
+// dots = sum of the partials; column j of H gets them (first pass) or adds
+// them. One CTA per possible dot product (grid m + 1, RT threads); CTAs past
+// ctl->j return at once.
+__global__ void __launch_bounds__(RT) reduce_parts_ctl(int nblocks, int ldp, const KryCtl* __restrict__ ctl,
+                                                       const double* __restrict__ part, double* __restrict__ dots,
+                                                       double* __restrict__ H, int first) {
+    const int i = blockIdx.x;
+    if (i > ctl->j) return;   // the same for every thread of the CTA
+    const double sum = sum_parts(nblocks, ldp, i, part);
+    if (threadIdx.x == 0) {
+        double* col = H + size_t(ctl->m + 1) * ctl->j;
         dots[i] = sum;
         col[i] = first ? sum : col[i] + sum;
     }
@@ -607,7 +627,7 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
     const int G = vgrid(n);
     auto dot = [&](const T* a, const T* c) {
         multidot<T><<<G, 256, 0, s>>>(n, 1, a == c ? a : a, c, K.part); IEMIC_COUNT_LAUNCH();
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
         ck(cudaMemcpyAsync(K.hpin, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
         ck(cudaStreamSynchronize(s));
         return K.hpin[0];
@@ -649,11 +669,11 @@ static int gmres(Engine& e, NdLu& lu, const int* rp, const int* ci, const T* val
             e.timer.stop(ev, s, IEMIC_KC_SPMV, spmv_bytes, 2.0 * double(e.nnz));
             for (int pass = 0; pass < 2; ++pass) {   // CGS2
                 multidot<T><<<G, 256, 0, s>>>(n, j + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
-                reduce_parts<<<1, 256, 0, s>>>(G, j + 1, K.part, K.dots, K.h, pass == 0); IEMIC_COUNT_LAUNCH();
+                reduce_parts<<<j + 1, RT, 0, s>>>(G, j + 1, K.part, K.dots, K.h, pass == 0); IEMIC_COUNT_LAUNCH();
                 basis_update<T><<<G, 256, 0, s>>>(n, j + 1, V, K.dots, w); IEMIC_COUNT_LAUNCH();
             }
             multidot<T><<<G, 256, 0, s>>>(n, 1, w, w, K.part); IEMIC_COUNT_LAUNCH();
-            reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0); IEMIC_COUNT_LAUNCH();
+            reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.h + j + 1, nullptr, 0); IEMIC_COUNT_LAUNCH();
             ck(cudaMemcpyAsync(K.hpin, K.h, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, s));
             ck(cudaStreamSynchronize(s));
             e.timer.drain();   // before the next replay re-records the graph's timing events
@@ -747,11 +767,11 @@ static bool ensure_cycle_graph(Engine& e, NdLu& lu, const int* rp, const int* ci
         spmv_launch<double>(n, rp, ci, vals, z, w, e.rowintcon, s);
         for (int pass = 0; pass < 2; ++pass) {   // CGS2
             multidot_ctl<<<G, 256, 0, s>>>(n, K.ctl, m + 1, V, w, K.part); IEMIC_COUNT_LAUNCH();
-            reduce_parts_ctl<<<1, 256, 0, s>>>(G, m + 1, K.ctl, K.part, K.dots, K.H, pass == 0); IEMIC_COUNT_LAUNCH();
+            reduce_parts_ctl<<<m + 1, RT, 0, s>>>(G, m + 1, K.ctl, K.part, K.dots, K.H, pass == 0); IEMIC_COUNT_LAUNCH();
             basis_update_ctl<<<G, 256, 0, s>>>(n, K.ctl, V, K.dots, w); IEMIC_COUNT_LAUNCH();
         }
         multidot<double><<<G, 256, 0, s>>>(n, 1, w, w, K.part); IEMIC_COUNT_LAUNCH();
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, &K.ctl->hn2, nullptr, 0); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, &K.ctl->hn2, nullptr, 0); IEMIC_COUNT_LAUNCH();
         k_givens<<<1, 32, 0, s>>>(K.ctl, K.H, K.cs, K.sn, K.g, cond); IEMIC_COUNT_LAUNCH();
         k_scale_next<<<G, 256, 0, s>>>(n, K.ctl, w, V, K.vcur); IEMIC_COUNT_LAUNCH();
     } catch (...) {
@@ -807,7 +827,7 @@ static bool gmres_dev(Engine& e, NdLu& lu, const int* rp, const int* ci, const d
     double* z = static_cast<double*>(K.z);
     auto norm = [&](const double* a) {
         multidot<double><<<G, 256, 0, s>>>(n, 1, a, a, K.part); IEMIC_COUNT_LAUNCH();
-        reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+        reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
         ck(cudaMemcpyAsync(K.hpin, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
         ck(cudaStreamSynchronize(s));
         return std::sqrt(K.hpin[0]);
@@ -878,7 +898,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     cudaStream_t s = stream;
     // ||b||
     multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part); IEMIC_COUNT_LAUNCH();
-    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double bn2 = 0.0;
     ck(cudaMemcpyAsync(&bn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
     ck(cudaStreamSynchronize(s));
@@ -902,7 +922,7 @@ int Engine::solve_dev(const double* b, double* x, const iemic_solve_opts& o, iem
     axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
     residual_launch(n, d_rowptr, d_col, d_val, x, b, K.r64, rowintcon, s);
     multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
-    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double rn2 = 0.0;
     ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
     ck(cudaStreamSynchronize(s));
@@ -974,7 +994,7 @@ int Engine::solve_transpose_dev(const double* b, double* x, const iemic_solve_op
     const int n = ndim, G = vgrid(n);
     cudaStream_t s = stream;
     multidot<double><<<G, 256, 0, s>>>(n, 1, b, b, K.part); IEMIC_COUNT_LAUNCH();
-    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double bn2 = 0.0;
     ck(cudaMemcpyAsync(&bn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
     ck(cudaStreamSynchronize(s));
@@ -992,7 +1012,7 @@ int Engine::solve_transpose_dev(const double* b, double* x, const iemic_solve_op
     axpy_into<double><<<G, 256, 0, s>>>(n, bnorm, K.x64, x); IEMIC_COUNT_LAUNCH();
     residual_launch(n, d_rowT, d_colT, d_valT, x, b, K.r64, -1, s);
     multidot<double><<<G, 256, 0, s>>>(n, 1, K.r64, K.r64, K.part); IEMIC_COUNT_LAUNCH();
-    reduce_parts<<<1, 32, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, RT, 0, s>>>(G, 1, K.part, K.dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double rn2 = 0.0;
     ck(cudaMemcpyAsync(&rn2, K.dots, sizeof(double), cudaMemcpyDeviceToHost, s));
     ck(cudaStreamSynchronize(s));
@@ -1017,7 +1037,7 @@ double dev_dot(Engine& e, const double* a, const double* b) {
     ensure_krylov(e, e.kry ? e.kry->m : 100, e.kry ? e.kry->prec : 0);
     const int n = e.ndim, G = vgrid(n);
     multidot<double><<<G, 256, 0, e.stream>>>(n, 1, a, b, e.kry->part); IEMIC_COUNT_LAUNCH();
-    reduce_parts<<<1, 32, 0, e.stream>>>(G, 1, e.kry->part, e.kry->dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
+    reduce_parts<<<1, RT, 0, e.stream>>>(G, 1, e.kry->part, e.kry->dots, nullptr, 0); IEMIC_COUNT_LAUNCH();
     double v = 0.0;
     ck(cudaMemcpyAsync(&v, e.kry->dots, sizeof(double), cudaMemcpyDeviceToHost, e.stream));
     ck(cudaStreamSynchronize(e.stream));

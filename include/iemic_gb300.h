@@ -254,7 +254,9 @@ typedef struct {
                                     the Krylov time spent beyond the first solve's iteration count
                                     exceeds the factorisation's own time; a solve on an older
                                     Jacobian's factors gets only the iterations that budget still
-                                    pays for, and is repeated on fresh factors if it runs out.
+                                    pays for, and is repeated on fresh factors if it runs out; after
+                                    such a failure the step's later Jacobians are factorised directly
+                                    when fresh factors need >= 8 iterations (inexact FP32 factors).
                                  Setting IEMIC_SOLVE_TRACE=1 in the environment prints one line per
                                  solve and per step to stderr. */
 } iemic_continuation_opts;
