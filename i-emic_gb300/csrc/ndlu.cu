@@ -1627,25 +1627,84 @@ __global__ void k_stage_reduce(const FrontDev* __restrict__ fronts, const int* _
     }
 }
 
-// Epilogues of the product sweeps, one thread per row of the front:
-//   forward  (F rows):  y = Linv11 P w_own -> W, WP;  u_B = w_B - (L21 Linv11) P w_own -> WP[B]
-//   backward (nf rows): x_own = Uinv11 y - (Uinv11 U12) x_B -> xred
-template <bool UP>
-__global__ void k_prod_reduce(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, StageBufs sb,
-                              double* __restrict__ W, double* __restrict__ WP, double* __restrict__ xred) {
-    const int f = lf[blockIdx.y];
-    const FrontDev fr = fronts[f];
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (UP) {
-        if (r >= fr.nf) return;
-        xred[fr.red0 + r] = stage_sum(ST_UINV, f, fr, r, sb) + stage_sum(ST_U12, f, fr, r, sb);
-    } else if (r < fr.nf) {
-        const double y = stage_sum(ST_LINV, f, fr, r, sb);
-        W[fr.woff + r] = y;
-        WP[fr.woff + r] = y;
-    } else if (r < fr.F) {
-        WP[fr.woff + r] += stage_sum(ST_L21, f, fr, r, sb);
+// Level links of the product sweeps: the epilogue of level h and the gather
+// of the next level in one launch (grid.y: the fronts of level h, then those
+// of the next level). The next level's gather adds a child's pending partial
+// sums itself when the child is at level h, so the two parts never touch the
+// same rows.
+//   forward, levels h -> h + 1:
+//     level h:      y -> W, WP (own rows); u_B = w_B + partials -> WP[B] only
+//                   for fronts whose parent is not at level h + 1 (those are
+//                   gathered later, from WP);
+//     level h + 1:  w = [red_own ; 0] + the children's update vectors, W = w,
+//                   WP = P w (own rows), as k_fwd_gather;
+//   backward, levels h -> h - 1:
+//     level h:      x_own = partials -> xred;
+//     level h - 1:  WP = [y ; x_B] as k_bwd_gather, x_B of an ancestor at
+//                   level h summed from its partials.
+// Sums are formed in the same order as the separate kernels', so results are
+// bit-identical to them.
+__device__ __forceinline__ double link_update(const FrontDev* __restrict__ fronts, int c, int a, int h,
+                                              const double* __restrict__ WP, const StageBufs& sb) {
+    const FrontDev ch = fronts[c];
+    const double u = WP[ch.woff + ch.nf + a];
+    return ch.lvl == h ? u + stage_sum(ST_L21, c, ch, ch.nf + a, sb) : u;
+}
+__device__ __forceinline__ double link_row(const FrontDev* __restrict__ fronts, const FrontDev& fr, int f, int q, int h,
+                                           const double* __restrict__ red, const int* __restrict__ child_of,
+                                           const int2* __restrict__ einv, const double* __restrict__ WP,
+                                           const StageBufs& sb) {
+    double w = q < fr.nf ? red[fr.red0 + q] : 0.0;
+    const int2 a = einv[fr.woff + q];
+    if (a.x >= 0) w += link_update(fronts, child_of[2 * f], a.x, h, WP, sb);
+    if (a.y >= 0) w += link_update(fronts, child_of[2 * f + 1], a.y, h, WP, sb);
+    return w;
+}
+__global__ void k_fwd_link(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int nfr, const int* __restrict__ lfn,
+                           int h, StageBufs sb, const int* __restrict__ child_of, const int2* __restrict__ einv,
+                           const int* __restrict__ piv, const double* __restrict__ red, double* __restrict__ W,
+                           double* __restrict__ WP, int B) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (int(blockIdx.y) < nfr) {
+        const int f = lf[blockIdx.y];
+        const FrontDev fr = fronts[f];
+        if (q < fr.nf) {
+            const double y = stage_sum(ST_LINV, f, fr, q, sb);
+            W[fr.woff + q] = y;
+            WP[fr.woff + q] = y;
+        } else if (q < fr.F && (fr.parent < 0 || fronts[fr.parent].lvl != h + 1)) {
+            WP[fr.woff + q] += stage_sum(ST_L21, f, fr, q, sb);
+        }
+        return;
     }
+    const int f = lfn[blockIdx.y - nfr];
+    const FrontDev fr = fronts[f];
+    if (q >= fr.F) return;
+    const double wq = link_row(fronts, fr, f, q, h, red, child_of, einv, WP, sb);
+    W[fr.woff + q] = wq;
+    WP[fr.woff + q] = q < fr.nf ? link_row(fronts, fr, f, piv_row(piv, fr, q, B), h, red, child_of, einv, WP, sb) : wq;
+}
+__global__ void k_bwd_link(const FrontDev* __restrict__ fronts, const int* __restrict__ lf, int nfr, const int* __restrict__ lfn,
+                           int h, StageBufs sb, const int* __restrict__ vars, const int* __restrict__ owner,
+                           const double* __restrict__ W, double* __restrict__ xred, double* __restrict__ WP) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (int(blockIdx.y) < nfr) {
+        const int f = lf[blockIdx.y];
+        const FrontDev fr = fronts[f];
+        if (q < fr.nf) xred[fr.red0 + q] = stage_sum(ST_UINV, f, fr, q, sb) + stage_sum(ST_U12, f, fr, q, sb);
+        return;
+    }
+    const FrontDev fr = fronts[lfn[blockIdx.y - nfr]];
+    if (q >= fr.F) return;
+    if (q < fr.nf) {
+        WP[fr.woff + q] = W[fr.woff + q];
+        return;
+    }
+    const int v = vars[fr.voff + q];
+    const int o = owner[v];
+    const FrontDev an = fronts[o];
+    WP[fr.woff + q] = an.lvl == h ? stage_sum(ST_UINV, o, an, v - an.red0, sb) + stage_sum(ST_U12, o, an, v - an.red0, sb)
+                                  : xred[v];
 }
 
 // backward prologue: X = [y ; x_B]
@@ -1962,6 +2021,12 @@ void ndlu_setup(NdLu& lu, const NdPlan& plan, int prec, int subst_min_nf) {
     lu.d_asm_dst = upload(lu, plan.asm_dst, s);
     lu.d_asm_row = upload(lu, plan.asm_row, s);
     lu.d_child_of = upload(lu, child_of, s);
+    {
+        std::vector<int> owner(size_t(std::max(plan.nred, 1)), -1);
+        for (int f = 0; f < plan.nfronts; ++f)
+            for (int q = 0; q < plan.fronts[f].nf; ++q) owner[size_t(plan.fronts[f].red0) + q] = f;
+        lu.d_owner = upload(lu, owner, s);
+    }
     lu.d_piv = static_cast<int*>(dmalloc(lu, sizeof(int) * size_t(std::max(plan.nred, 1))));
     lu.d_front = dmalloc(lu, ts * size_t(plan.work_entries));
     lu.d_factor = dmalloc(lu, ts * size_t(std::max<int64_t>(plan.factor_entries, 1)));
@@ -2618,28 +2683,36 @@ static void launch_group(NdLu& lu, int g, int h, const T* front, double* WP, cud
     if (ev) lu.timer->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.group_bytes[g][h], 2.0 * lu.group_bytes[g][h] / sizeof(T));
 }
 // one GEMV launch of the product sweeps (g = 0 forward, 1 backward) over
-// level h, both stages of the level, and its epilogue
+// level h: both stages of the level
 template <class T>
-static void launch_mgroup(NdLu& lu, int g, int h, double* W, double* WP, double* red, cudaStream_t s) {
-    const NdPlan& P = *lu.plan;
+static void launch_mgemv(NdLu& lu, int g, int h, double* WP, cudaStream_t s) {
     KTimer* kt = lu.timer;
     const int ni = lu.mgroup_start[g][h + 1] - lu.mgroup_start[g][h];
-    if (ni > 0) {
-        cudaEvent_t ev = kt ? kt->start(s) : nullptr;
-        k_gemv_part<T><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_mgroup_items[g]) +
-                                             lu.mgroup_start[g][h], static_cast<const T*>(lu.d_factor),
-                                         static_cast<const T*>(lu.d_prod), WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
-        if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.mgroup_bytes[g][h], 2.0 * lu.mgroup_bytes[g][h] / sizeof(T));
-    }
+    if (ni <= 0) return;
+    cudaEvent_t ev = kt ? kt->start(s) : nullptr;
+    k_gemv_part<T><<<ni, GR, 0, s>>>(lu.d_fronts, static_cast<const WorkItem*>(lu.d_mgroup_items[g]) +
+                                         lu.mgroup_start[g][h], static_cast<const T*>(lu.d_factor),
+                                     static_cast<const T*>(lu.d_prod), WP, stage_bufs(lu)); IEMIC_COUNT_LAUNCH();
+    if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_GEMV, lu.mgroup_bytes[g][h], 2.0 * lu.mgroup_bytes[g][h] / sizeof(T));
+}
+// the level link after level h's GEMV: its epilogue and the gather of the
+// next level hn (forward h + 1, backward h - 1; -1: none, the sweep's end)
+static void launch_link(NdLu& lu, bool up, int h, int hn, double* W, double* WP, double* red, int B, cudaStream_t s) {
+    const NdPlan& P = *lu.plan;
+    KTimer* kt = lu.timer;
     const int nfr = lu.level_start[h + 1] - lu.level_start[h];
     const int* lf = lu.d_level_fronts + lu.level_start[h];
-    const int rows = g == 0 ? P.level_maxF[h] : P.level_maxnf[h];
-    if (rows <= 0) return;
+    const int nfn = hn >= 0 ? lu.level_start[hn + 1] - lu.level_start[hn] : 0;
+    const int* lfn = hn >= 0 ? lu.d_level_fronts + lu.level_start[hn] : nullptr;
+    const int rows = std::max(up ? P.level_maxnf[h] : P.level_maxF[h], hn >= 0 ? P.level_maxF[hn] : 0);
+    if (rows <= 0 || nfr + nfn <= 0) return;
     cudaEvent_t ev = kt ? kt->start(s) : nullptr;
-    if (g == 0)
-        k_prod_reduce<false><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red);
+    const dim3 grid((rows + NT - 1) / NT, nfr + nfn);
+    if (up)
+        k_bwd_link<<<grid, NT, 0, s>>>(lu.d_fronts, lf, nfr, lfn, h, stage_bufs(lu), lu.d_vars, lu.d_owner, W, red, WP);
     else
-        k_prod_reduce<true><<<dim3((rows + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, stage_bufs(lu), W, WP, red);
+        k_fwd_link<<<grid, NT, 0, s>>>(lu.d_fronts, lf, nfr, lfn, h, stage_bufs(lu), lu.d_child_of, lu.d_einv, lu.d_piv,
+                                       red, W, WP, B);
     IEMIC_COUNT_LAUNCH();
     if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
 }
@@ -2694,17 +2767,19 @@ static void sweeps_t(NdLu& lu, int mode, cudaStream_t s) {
     double* WP = static_cast<double*>(lu.d_wp);
     const T* front = static_cast<const T*>(lu.d_factor);
     KTimer* kt = lu.timer;
+    const int top = P.nlevels - 1;
     for (int h = 0; h < P.nlevels; ++h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
-        {
+        if (!prod || h == 0) {
             cudaEvent_t ev = kt ? kt->start(s) : nullptr;
             k_fwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_child_of,
                                                                                 lu.d_einv, lu.d_piv, red, W, WP, B); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        if (prod) {   // both stages in one launch, one epilogue
-            launch_mgroup<T>(lu, 0, h, W, WP, red, s);
+        if (prod) {   // both stages in one launch, then the link to the next level
+            launch_mgemv<T>(lu, 0, h, WP, s);
+            launch_link(lu, false, h, h < top ? h + 1 : -1, W, WP, red, B, s);
             continue;
         }
         if (full) {
@@ -2719,13 +2794,14 @@ static void sweeps_t(NdLu& lu, int mode, cudaStream_t s) {
     for (int h = P.nlevels - 1; h >= 0; --h) {
         const int nfr = lu.level_start[h + 1] - lu.level_start[h];
         const int* lf = lu.d_level_fronts + lu.level_start[h];
-        {
+        if (!prod || h == top) {
             cudaEvent_t ev = kt ? kt->start(s) : nullptr;
             k_bwd_gather<<<dim3((P.level_maxF[h] + NT - 1) / NT, nfr), NT, 0, s>>>(lu.d_fronts, lf, lu.d_vars, W, red, WP); IEMIC_COUNT_LAUNCH();
             if (ev) kt->stop(ev, s, IEMIC_KC_SOLVE_OTHER, 0.0, 0.0);
         }
-        if (prod) {   // both stages in one launch, one epilogue
-            launch_mgroup<T>(lu, 1, h, W, WP, red, s);
+        if (prod) {   // both stages in one launch, then the link to the next level
+            launch_mgemv<T>(lu, 1, h, WP, s);
+            launch_link(lu, true, h, h > 0 ? h - 1 : -1, W, WP, red, B, s);
             continue;
         }
         launch_group<T>(lu, 2, h, front, WP, s);

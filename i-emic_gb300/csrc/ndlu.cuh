@@ -76,6 +76,7 @@ struct NdLu {
     char* d_isdry = nullptr;                // 1 for unknowns left out of the factorisation
     int *d_dry_ptr = nullptr, *d_dry_e = nullptr, *d_dry_c = nullptr;   // NdPlan::dry_*
     int2* d_einv = nullptr;                 // per solve-vector row: child update rows (slot 0, slot 1) or -1
+    int* d_owner = nullptr;                 // per reduced unknown: the front whose own unknown it is
     int* d_asm_src = nullptr;
     int* d_asm_row = nullptr;
     double *d_dr = nullptr, *d_dc = nullptr, *d_cmax = nullptr;   // equilibration scalings
