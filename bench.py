@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=1, help="Newton iterations of the CPU sample")
     ap.add_argument("--ref-steps", type=int, default=2,
                     help="continuation steps the reference arm (CPU port) times at most")
-    ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1", "newton_large"],
+    ap.add_argument("--dt", type=float, default=0.05, help="transient: time step of the theta method")
+    ap.add_argument("--mode", default="continuation", choices=["continuation", "newton1", "newton_large", "transient"],
                     help="newton1: one Newton iteration per precision from the seeded state, per-kernel-class "
                          "device times (a short case for profiling); newton_large: Newton iterations on the "
                          "360x160x20 ocean with per-kernel HBM rates")
@@ -529,6 +530,53 @@ def run_newton1(args):
     print(json.dumps(out), flush=True)
 
 
+def run_transient(args):
+    """Implicit time steps (theta = 1, ThetaModel<Ocean> + transient Newton)
+    after a jump of the freshwater forcing: the steady state at Combined
+    Forcing --setup-comb, Salinity Forcing raised by 0.1, then --warmup
+    untimed and --steps timed steps of size --dt, per precision, through the
+    public host-buffer API (state copied in and out every step)."""
+    import torch
+    from iemic import Ocean
+    from iemic import workloads as W
+    torch.cuda.init()
+    cfg, lm, frc = workload(args.workload)
+    oc = Ocean(cfg, lm, forcing=frc, starting_parameters=W.STARTING_PARAMETERS)
+    nd = oc.ndim
+    fscale = float(np.linalg.norm(oc.computeRHS(np.zeros(nd))))
+    oc.setPar("Combined Forcing", 0.0)
+    x0, st0 = oc.continuation(np.zeros(nd), par="Combined Forcing", precision=1, ds=args.setup_comb / 2,
+                              ds_max=args.setup_comb, destination=args.setup_comb, max_steps=20,
+                              newton_tol=1e-8 * fscale, residual_test=b"R", predictor_bound=1e30)
+    if st0["status"] != 0 or not st0["reached_destination"]:
+        raise RuntimeError("setup continuation failed: %s" % st0)
+    oc.setPar("Salinity Forcing", oc.getPar("Salinity Forcing") + 0.1)
+    out = {"mode": "transient", "workload": args.workload, "dt": args.dt, "theta": 1.0, "steps": args.steps,
+           "warmup": args.warmup, "unknowns": nd}
+    for label, prec in (("mixed", 1), ("fp64", 0)):
+        x = x0.copy()
+        for _ in range(args.warmup):
+            x, _ = oc.thetaStep(x, dt=args.dt, theta=1.0, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sts = []
+        for _ in range(args.steps):
+            x, s = oc.thetaStep(x, dt=args.dt, theta=1.0, precision=prec)
+            sts.append(s)
+        wall = time.perf_counter() - t0
+        out[label] = {"time_steps_per_s": args.steps / wall, "wall_s": wall,
+                      "converged_steps": sum(s["converged"] for s in sts),
+                      "newton_iters": sum(s["newton_iters"] for s in sts),
+                      "krylov_iters": sum(s["krylov_iters"] for s in sts),
+                      "factorizations": sum(s["factorizations"] for s in sts),
+                      "factor_ms": sum(s["time_factor_ms"] for s in sts),
+                      "solve_ms": sum(s["time_solve_ms"] for s in sts),
+                      "last_norm_G": sts[-1]["norm_G"] if sts else None}
+    if out["fp64"]["wall_s"] > 0:
+        out["speedup_vs_fp64_gpu"] = out["mixed"]["time_steps_per_s"] / out["fp64"]["time_steps_per_s"]
+    print(json.dumps(out), flush=True)
+
+
 def run_newton_large(args):
     """Newton iterations on the 1-degree 360x160x20 ocean (6.9 M unknowns):
     iteration 0 with every kernel timed (per-class device time and HBM rate),
@@ -610,6 +658,9 @@ def main():
         return
     if args.mode == "newton1":
         run_newton1(args)
+        return
+    if args.mode == "transient":
+        run_transient(args)
         return
     rank, world = dist_init()
     if args.impl == "reference":

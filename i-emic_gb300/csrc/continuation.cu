@@ -446,6 +446,46 @@ struct Continuation {
     }
 };
 
+// ---- theta method (ThetaModel<Ocean>, src/transient/ThetaModel.H:64-140) ----
+// G = B (x_old - x) + (dt (1 - theta) F_old + dt theta F), in the order of the
+// Epetra updates of ThetaModel::computeRHS (unfused products and sums)
+__global__ void k_theta_rhs(int n, const double* __restrict__ B, const double* __restrict__ xold,
+                            const double* __restrict__ x, const double* __restrict__ Fold, double a, double b,
+                            double* __restrict__ FG) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const double bxdot = __dmul_rn(B[r], __dadd_rn(-x[r], xold[r]));
+        const double f = __dadd_rn(__dmul_rn(a, Fold[r]), __dmul_rn(b, FG[r]));
+        FG[r] = __dadd_rn(bxdot, f);
+    }
+}
+// J2 = J - B / (theta dt) on the diagonal (ThetaModel::computeJacobian)
+__global__ void k_theta_diag(int n, const int* __restrict__ diagpos, const double* __restrict__ B, double dt,
+                             double theta, double* __restrict__ val) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int q = diagpos[r];
+        if (q >= 0) val[q] = __dadd_rn(val[q], -B[r] / dt / theta);
+    }
+}
+__global__ void k_scale(int n, double s, const double* __restrict__ x, double* __restrict__ y) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) y[r] = __dmul_rn(x[r], s);
+}
+int vblocks(int n) { return std::min((n + 255) / 256, 152 * 8); }
+
+// CSR position of each row's diagonal entry (-1 if the maximal graph has none)
+const int* diag_positions(Engine& e) {
+    if (!e.d_diagpos) {
+        const std::vector<int>& ci = e.host_col_idx();
+        std::vector<int> pos(size_t(e.ndim), -1);
+        for (int r = 0; r < e.ndim; ++r)
+            for (int q = e.row_ptr[r]; q < e.row_ptr[r + 1]; ++q)
+                if (ci[q] == r) pos[r] = q;
+        e.d_diagpos = static_cast<int*>(e.dalloc(sizeof(int) * pos.size()));
+        ck(cudaMemcpyAsync(e.d_diagpos, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice, e.stream));
+        ck(cudaStreamSynchronize(e.stream));
+    }
+    return e.d_diagpos;
+}
+
 }  // namespace
 
 extern "C" {
@@ -613,6 +653,92 @@ int iemic_continuation_run(iemic_ocean* h, double* x, const iemic_continuation_o
                            iemic_continuation_stats* st) {
     if (!h || !x) return IEMIC_ERR_ARG;
     return with_device_state(h, x, [&](double* d) { return iemic_continuation_run_dev(h, d, opts, st); });
+}
+
+void iemic_default_theta_opts(iemic_theta_opts* o) {
+    if (!o) return;
+    o->theta = 1.0;        // ThetaModel "theta"
+    o->dt = 1.0e-3;        // ThetaModel::timestep_ before initStep
+    o->tol = 1.0e-8;       // transient Newton "Newton tolerance"
+    o->max_newton = 20;    // "maximum Newton iterations"
+    iemic_default_solve_opts(&o->solve);
+    o->refactor_policy = 2;
+}
+
+// ThetaModel::initStep + Newton<ThetaModel>::run (src/transient/Newton.H:77-110)
+int iemic_theta_step_dev(iemic_ocean* h, double* x, const iemic_theta_opts* opts, iemic_theta_stats* st) {
+    if (!h || !x) return IEMIC_ERR_ARG;
+    iemic_theta_opts o;
+    iemic_default_theta_opts(&o);
+    if (opts) o = *opts;
+    if (!(o.theta > 0.0 && o.theta <= 1.0) || !(o.dt > 0.0) || o.max_newton < 0 || o.refactor_policy < 0 ||
+        o.refactor_policy > 2)
+        return IEMIC_ERR_ARG;
+    iemic_theta_stats s{};
+    Engine& e = h->e;
+    int rc = IEMIC_OK;
+    auto t0 = clk::now();
+    try {
+        DevVecs V(e, 4);
+        double *xold = V.v[0], *Fold = V.v[1], *G = V.v[2], *dx = V.v[3];
+        ModelOps M(e, o.solve, o.refactor_policy);
+        const int* diagpos = diag_positions(e);
+        const int n = e.ndim, nb = vblocks(n);
+        const double a = o.dt * (1.0 - o.theta), b = o.dt * o.theta, scale = 1.0 / o.dt / o.theta;
+        // initStep: the old state, Ocean::preProcess, F(x_old)
+        M.copy(xold, x);
+        M.pre_process();
+        M.rhs(xold, Fold);
+        auto residual = [&](const double* xc) {   // G(xc), ThetaModel::computeRHS
+            M.rhs(xc, G);
+            k_theta_rhs<<<nb, 256, 0, e.stream>>>(n, e.d_B, xold, xc, Fold, a, b, G); IEMIC_COUNT_LAUNCH();
+            ck(cudaGetLastError());
+        };
+        residual(x);
+        s.norm_G = -1.0;
+        double gnorm = M.norm(G);
+        for (s.newton_iters = 0; s.newton_iters < o.max_newton;) {
+            // Jsol: J2 at x, J2 dx = G / (theta dt). The linear tolerance is
+            // relaxed to what the Newton test needs: a linear residual below
+            // 0.1 tol in G's units; near convergence G is at round-off level
+            // and a 1e-8 relative solve of it is neither reachable nor needed.
+            M.solve_opts.tol = gnorm > 0.0 ? std::max(o.solve.tol, 0.1 * o.tol / gnorm) : o.solve.tol;
+            M.jacobian(x);
+            k_theta_diag<<<nb, 256, 0, e.stream>>>(n, diagpos, e.d_B, o.dt, o.theta, e.d_val); IEMIC_COUNT_LAUNCH();
+            k_scale<<<nb, 256, 0, e.stream>>>(n, scale, G, G); IEMIC_COUNT_LAUNCH();
+            M.solve(G, dx);
+            s.norm_dx = M.norm_inf(dx);
+            M.axpby(-1.0, dx, 1.0, x);
+            residual(x);
+            s.norm_G = gnorm = M.norm(G);
+            ++s.newton_iters;
+            if (!std::isfinite(s.norm_G) || !std::isfinite(s.norm_dx)) throw EngineError(IEMIC_ERR_NAN);
+            if (s.norm_dx < o.tol && s.norm_G < o.tol) {
+                s.converged = 1;
+                break;
+            }
+            if (s.norm_dx > 1e2) break;   // "Norm exploding"
+        }
+        if (!s.converged) rc = IEMIC_ERR_NOT_CONVERGED;
+        s.linear_solves = M.solves;
+        s.krylov_iters = M.krylov;
+        s.factorizations = M.facts;
+        s.time_assembly_ms = M.t_asm;
+        s.time_factor_ms = M.t_fac;
+        s.time_solve_ms = M.t_sol;
+    } catch (const EngineError& err) {
+        rc = err.code;
+    } catch (...) {
+        rc = IEMIC_ERR_CUDA;
+    }
+    s.time_ms = ms_since(t0);
+    if (st) *st = s;
+    return rc;
+}
+
+int iemic_theta_step(iemic_ocean* h, double* x, const iemic_theta_opts* opts, iemic_theta_stats* st) {
+    if (!h || !x) return IEMIC_ERR_ARG;
+    return with_device_state(h, x, [&](double* d) { return iemic_theta_step_dev(h, d, opts, st); });
 }
 
 }  // extern "C"

@@ -47,6 +47,7 @@ struct Engine {
     int8_t* d_slot = nullptr;
     double *d_jt = nullptr, *d_kt = nullptr, *d_al = nullptr, *d_pads = nullptr, *d_surf = nullptr;
     double *d_x = nullptr, *d_F = nullptr, *d_v1 = nullptr, *d_v2 = nullptr, *d_B = nullptr;
+    int* d_diagpos = nullptr;   // CSR position of each row's diagonal (theta method), built on first use
     int device = 0;           // the CUDA device the handle was created on
     // vertical mixing (Mixing >= 1): partition flags (device) and norm partials
     int* d_mixflags = nullptr;

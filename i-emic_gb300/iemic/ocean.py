@@ -76,6 +76,19 @@ class NewtonStats(ctypes.Structure):
                 ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
 
 
+class ThetaOpts(ctypes.Structure):
+    _fields_ = [("theta", ctypes.c_double), ("dt", ctypes.c_double), ("tol", ctypes.c_double),
+                ("max_newton", ctypes.c_int), ("solve", SolveOpts), ("refactor_policy", ctypes.c_int)]
+
+
+class ThetaStats(ctypes.Structure):
+    _fields_ = [("newton_iters", ctypes.c_int), ("converged", ctypes.c_int), ("linear_solves", ctypes.c_int),
+                ("krylov_iters", ctypes.c_int), ("factorizations", ctypes.c_int),
+                ("norm_G", ctypes.c_double), ("norm_dx", ctypes.c_double),
+                ("time_ms", ctypes.c_double), ("time_assembly_ms", ctypes.c_double),
+                ("time_factor_ms", ctypes.c_double), ("time_solve_ms", ctypes.c_double)]
+
+
 class ContinuationOpts(ctypes.Structure):
     _fields_ = [("par_idx", ctypes.c_int), ("ds", ctypes.c_double), ("ds_min", ctypes.c_double),
                 ("ds_max", ctypes.c_double), ("decrease", ctypes.c_double),
@@ -173,6 +186,9 @@ SIGNATURES = {
     "iemic_default_newton_opts": [ctypes.POINTER(NewtonOpts)],
     "iemic_newton": [_VP, _DP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonStats)],
     "iemic_newton_dev": [_VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonStats)],
+    "iemic_default_theta_opts": [ctypes.POINTER(ThetaOpts)],
+    "iemic_theta_step": [_VP, _DP, ctypes.POINTER(ThetaOpts), ctypes.POINTER(ThetaStats)],
+    "iemic_theta_step_dev": [_VP, _VP, ctypes.POINTER(ThetaOpts), ctypes.POINTER(ThetaStats)],
     "iemic_default_continuation_opts": [ctypes.POINTER(ContinuationOpts)],
     "iemic_continuation_run": [_VP, _DP, ctypes.POINTER(ContinuationOpts), ctypes.POINTER(ContinuationStats)],
     "iemic_continuation_run_dev": [_VP, _VP, ctypes.POINTER(ContinuationOpts),
@@ -185,7 +201,7 @@ SIGNATURES = {
     "iemic_kernel_trace": [_VP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float), _DP, _IP],
 }
 _VOID_RETURN = {"iemic_default_solve_opts", "iemic_default_newton_opts", "iemic_default_continuation_opts",
-                "iemic_default_adjoint_opts"}
+                "iemic_default_adjoint_opts", "iemic_default_theta_opts"}
 
 _lib = None
 
@@ -431,6 +447,34 @@ class Ocean:
         stats["status"] = rc
         if rc not in (0, -3):
             raise IemicError(rc, "newton")
+        self.state[:] = x
+        return x, stats
+
+    # ---- implicit time stepping (src/transient/ThetaModel.H, src/transient/Newton.H)
+    def default_theta_opts(self, precision=PREC_MIXED):
+        o = ThetaOpts()
+        self.L.iemic_default_theta_opts(ctypes.byref(o))
+        o.solve.precision = precision
+        return o
+
+    def thetaStep(self, x=None, dt=None, theta=None, opts=None, **kw):
+        """One implicit theta-method step of size dt from x (default: the
+        stored state), ThetaModel<Ocean>::initStep + Newton::run. Returns
+        (x_new, stats); x_new also becomes the stored state."""
+        x = np.array(self.state if x is None else x, dtype=np.float64)
+        o = opts if opts is not None else self.default_theta_opts(kw.pop("precision", PREC_MIXED))
+        if dt is not None:
+            o.dt = dt
+        if theta is not None:
+            o.theta = theta
+        for k, v in kw.items():
+            setattr(o, k, v)
+        st = ThetaStats()
+        rc = self.L.iemic_theta_step(self._h, _dp(x), ctypes.byref(o), ctypes.byref(st))
+        stats = _asdict(st)
+        stats["status"] = rc
+        if rc not in (0, -3):
+            raise IemicError(rc, "thetaStep")
         self.state[:] = x
         return x, stats
 

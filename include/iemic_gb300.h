@@ -218,6 +218,40 @@ void iemic_default_newton_opts(iemic_newton_opts* o);
 int iemic_newton(iemic_ocean* h, double* x, const iemic_newton_opts* o, iemic_newton_stats* st);
 int iemic_newton_dev(iemic_ocean* h, double* x_dev, const iemic_newton_opts* o, iemic_newton_stats* st);
 
+/* One implicit time step of the theta method, ThetaModel<Ocean>
+ * (src/transient/ThetaModel.H:64-140) solved by the transient Newton
+ * iteration (src/transient/Newton.H:77-110). From x_old = x (in/out):
+ *   G(x) = B (x_old - x) + dt theta F(x) + dt (1 - theta) F(x_old)
+ *   J2   = J - B / (theta dt),   J2 dx = G / (theta dt),   x -= dx
+ * with B the diagonal mass matrix (iemic_mass), until ||dx||_inf < tol and
+ * ||G||_2 < tol; ||dx||_inf > 1e2 stops the iteration as diverging. The
+ * preconditioner follows `refactor_policy` (0: rebuilt once per time step, as
+ * ThetaModel::initStep calls Ocean::preProcess; 1: every iteration; 2: as
+ * refactor_each_newton = 2). Each linear solve runs to the relative
+ * tolerance solve.tol, relaxed to 0.1 tol / ||G||_2 when that is larger (the
+ * Newton test needs no more; near convergence G is at round-off level).
+ * theta must lie in (0, 1]: the explicit theta = 0
+ * division by B is not offered (B vanishes on land and pressure rows). The
+ * Jacobian left in the handle afterwards is J2 of the last iterate. */
+typedef struct {
+    double theta;             /* "theta" (1: backward Euler) */
+    double dt;                /* time step (the reference's timestep_) */
+    double tol;               /* "Newton tolerance" (1e-8) */
+    int max_newton;           /* "maximum Newton iterations" (20) */
+    iemic_solve_opts solve;
+    int refactor_policy;      /* 0, 1 or 2 (default 2) */
+} iemic_theta_opts;
+typedef struct {
+    int newton_iters, converged, linear_solves, krylov_iters, factorizations;
+    double norm_G, norm_dx;   /* ||G||_2 and ||dx||_inf of the last iteration */
+    double time_ms, time_assembly_ms, time_factor_ms, time_solve_ms;
+} iemic_theta_stats;
+void iemic_default_theta_opts(iemic_theta_opts* o);
+/* IEMIC_ERR_NOT_CONVERGED: the iteration cap was reached or it diverged;
+ * x then holds the last iterate. */
+int iemic_theta_step(iemic_ocean* h, double* x, const iemic_theta_opts* o, iemic_theta_stats* st);
+int iemic_theta_step_dev(iemic_ocean* h, double* x_dev, const iemic_theta_opts* o, iemic_theta_stats* st);
+
 /* Pseudo-arclength continuation (Continuation<Model>::run,
  * src/continuation/Continuation.H:209-1115). Field names follow the
  * reference's "Continuation parameters" list; defaults
