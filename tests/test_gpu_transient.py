@@ -69,3 +69,24 @@ def test_bad_arguments():
     for kw in (dict(theta=0.0), dict(theta=1.5), dict(dt=0.0), dict(dt=-1e-2)):
         with pytest.raises(IemicError):
             g.thetaStep(x, **{**dict(dt=1e-2, theta=1.0), **kw})
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_step_with_integral_condition_matches_oracle(prec):
+    """SRES = 0 (the reference's unit-test ocean, Mixing 1): the dense
+    integral-condition row has no mass, so J2 keeps it as in J."""
+    from iemic import workloads as W
+    from helpers import natl8_case
+    from oracle.transient import theta_step
+    cfg, lm, _ = natl8_case()
+    g = make_gpu(cfg, lm, None, W.NATL8_STARTING_PARAMETERS)
+    o = make_oracle(cfg, lm, None, W.NATL8_STARTING_PARAMETERS)
+    o.set_par("COMB", 0.5)
+    g.setPar("Combined Forcing", 0.5)
+    x = seeded_state(cfg, 2)
+    pins = g.getGauge()
+    xo, so = theta_step(o, x, 1e-2, 1.0, pins=pins)
+    xg, sg = g.thetaStep(x, dt=1e-2, theta=1.0, precision=prec)
+    assert sg["converged"] == 1 and so["converged"] == 1, (sg, so)
+    assert abs(sg["newton_iters"] - so["newton_iters"]) <= 1, (sg, so)
+    assert np.linalg.norm(xg - xo) <= 1e-7 * np.linalg.norm(xo), np.linalg.norm(xg - xo) / np.linalg.norm(xo)
